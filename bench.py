@@ -1,0 +1,264 @@
+#!/usr/bin/env python
+"""Throughput of the calcIR hot path on GB300: frame-steps per second.
+
+A frame-step is one frame of one time origin: field + Hamiltonian build, eigensolve,
+frequency distribution, propagation of F and the IR/Raman correlation contraction.
+One bench step is one whole job of the full-size configuration: 512 rigid TIP4P/2005
+molecules (1024 chromophores) in a 2.4834 nm box, 10 time origins 2 ps apart x 250
+correlation points at 10 fs = 2500 frame-steps, on seeded synthetic frames.
+
+  value  frame-steps/s with the positions already resident in HBM (cir_run on device
+         pointers), device time by CUDA events on the library's stream
+  e2e    the same through cir_run with pinned host buffers: positions copied in and all
+         results copied out inside the timed region
+
+--impl reference times the reference's per-frame algorithm (build, ssyevd, three complex
+GEMMs, 15 gemv/dot pairs) on the host cores, the only form of the reference that runs on
+the GPU machine (it needs MAGMA and libxdrfile, which are not installed there).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s (H build+eig+propagate) @512 H2O, mixed vs FP32, ≤1e-3 spectrum err"
+UNIT = "frames/s"
+NMOL = 512
+JOB = dict(model="tip4p2005", species="H2O", ntcfpoints=250, nsamples=10, sampleEvery=2.0, dt=0.010, t1=0.260,
+           avef=3415.0, omegaStart=2000, omegaStop=5000, omegaStep=1, nzeros=25600, map=0)
+WORKLOAD = ("512 TIP4P/2005 molecules (1024 chromophores, box 2.4834 nm), 10 time origins 2 ps apart x 250 "
+            "correlation points at 10 fs = 2500 frame-steps per step")
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.proc = None
+        try:
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+            if gpu_id is not None:
+                cmd += ["-i", str(gpu_id)]
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() in ("active", "0x1") or v == "1":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def gpu_identifier():
+    try:
+        import torch
+        props = torch.cuda.get_device_properties(torch.cuda.current_device())
+        uuid = getattr(props, "uuid", None)
+        if uuid:
+            s = str(uuid)
+            return s if s.startswith("GPU-") else "GPU-" + s
+    except Exception:
+        pass
+    return None
+
+
+def make_frames(cg, seed):
+    p = cg.default_params(**JOB)
+    fos = cg.frame_table(p, 0.010)
+    xyz, box = cg.synth_trajectory(NMOL, int(fos.max()) + 1, seed=seed)
+    return p, xyz, box, fos
+
+
+def cpu_port_rate(seed, steps_per_sample, repeats):
+    """Frame-steps/s of the reference algorithm on the host cores (oracle/cpu_reference)."""
+    import calcir_gb300 as cg
+    from oracle import cpu_reference as R
+    xyz, box = cg.synth_trajectory(NMOL, steps_per_sample, seed=seed)
+    prm = {"natom_mol": 4, "nchrom_mol": 2, "imodel": 1, "ispecies": 0, "map": 0, "avef": JOB["avef"],
+           "dt": JOB["dt"]}
+    R.time_frame_steps(xyz, box, prm, 2)   # warm-up (threads, page faults)
+    rates = []
+    for _ in range(repeats):
+        sec, cores = R.time_frame_steps(xyz, box, prm, steps_per_sample)
+        rates.append(steps_per_sample / sec)
+    return rates, R.host_cores()
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    per = args.cpu_sample
+    warm, _ = cpu_port_rate(args.seed, per, max(args.warmup, 0))
+    rates, cores = cpu_port_rate(args.seed, per, args.steps)
+    value = float(np.mean(rates))
+    sample = (f"{per} consecutive frame-steps of one origin of the workload (1024 chromophores) per step, "
+              "numpy FP32 ssyevd + complex64 GEMMs on the host cores")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "reference algorithm on the host CPU"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16x3"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-sample", type=int, default=8, help="frame-steps per CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from calcir_gb300 import build
+    build.build()
+    import calcir_gb300 as cg
+
+    # weak scaling: every rank runs its own 10-origin job on its own seeded trajectory
+    p, xyz, box, fos = make_frames(cg, args.seed + rank)
+    p.precision = cg.PREC[args.precision] if hasattr(cg, "PREC") else 0
+    steps_per_job = len(fos)
+    stream = torch.cuda.current_stream()
+    d_xyz = torch.from_numpy(xyz).cuda()
+    d_box = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(box, (xyz.shape[0], 3)))).cuda()
+    h_xyz = torch.from_numpy(xyz).pin_memory()
+    h_box = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(box, (xyz.shape[0], 3)))).pin_memory()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    with cg.Engine(p, xyz.shape[1]) as eng:
+        eng.set_stream(stream.cuda_stream)
+        for _ in range(max(args.warmup, 3)):
+            eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+        eng.reset_stats()
+        torch.cuda.synchronize()
+        barrier()
+        clocks = ClockSampler(gpu_identifier())
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+        t1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        clk = clocks.stop()
+        ms = t0.elapsed_time(t1)
+        st = eng.stats()
+        # end to end: pinned host positions in, all results out, inside the timed region
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            eng.run(h_xyz.data_ptr(), h_box.data_ptr(), fos, nframes=xyz.shape[0])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms_e2e = e0.elapsed_time(e1)
+
+    if world > 1:
+        t = torch.tensor([ms, ms_e2e], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, ms_e2e = t.tolist()
+    total_steps = steps_per_job * args.steps * world
+    value = total_steps / (ms * 1e-3)
+    e2e = total_steps / (ms_e2e * 1e-3)
+
+    n = NMOL * 2
+    pk, pk_kind = peaks()
+    eig_ms_per_launch = st["ms_eig"] / args.steps          # one eigensolver launch per job (one chunk)
+    eig_flops = 14.0 / 3.0 * n ** 3 * steps_per_job         # algorithmic flops per launch
+    achieved = eig_flops / (eig_ms_per_launch * 1e-3) / 1e12
+    nfft = JOB["ntcfpoints"] + JOB["nzeros"]
+    nomega = 3001
+    h2d = xyz.nbytes + xyz.shape[0] * 12 + fos.nbytes
+    d2h = steps_per_job * 48 + nomega * 8 * 4 + 3 * nfft * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": f"plain ({args.precision})", "nsamples": 10, "ntcfpoints": 250,
+                   "nchrom": n, "l2": "no flush needed: each step streams ~20 GB of Hamiltonians and eigenvectors "
+                                     "(>> 129 MB L2)"},
+        "stages_ms_per_step": {k: st[k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(st["kernel_launches"]),
+        "roofline": {"kernel": "k_eigh (batched eigensolver)", "bound": "tensor", "achieved": achieved,
+                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
+                     "peak_kind": f"{pk_kind} bf16 dense (no FP32-SIMT peak is recorded)",
+                     "work": "14/3 N^3 flops per matrix x 2500 matrices per launch", "traffic": None},
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rates, cores = cpu_port_rate(args.seed, args.cpu_sample, 2)
+        line["cpu_baseline"] = {"value": float(np.mean(rates)), "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"2 x {args.cpu_sample} frame-steps of one origin (1024 chromophores), "
+                                          "reference algorithm in numpy FP32 on the host cores"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,692 @@
+// C ABI of the engine: context, stage entry points and the whole-job driver cir_run.
+//
+// cir_run processes the nsamples x ntcfpoints frame-steps of a job in chunks of
+// consecutive steps for all time origins at once:
+//   1. gather the chunk's frames, build every Hamiltonian (one launch pair),
+//   2. diagonalise all of them (one batched launch; the frequency distribution of every
+//      eigenvector is binned in the same kernel),
+//   3. at step 0 of every origin: spectral density,
+//   4. for each step: propagate the F of every origin (two batched GEMMs) and contract
+//      the correlation terms (one launch).
+// The reference runs the same steps frame by frame with host round trips in between
+// (calcIR.cu:360-760): the eigenvalues come back to the host from ssyevd, the
+// eigenvectors are copied to the host every frame for the frequency distribution, and
+// every one of the 15 correlation dot products returns a scalar to the host.  Here
+// nothing leaves the device until the job ends.
+#include "cir_device.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+enum {
+    B_IN0, B_IN1, B_IN2, B_IN3, B_IN4, B_IN5,      // staging of host arguments
+    B_CT, B_Z, B_STATUS, B_SCR,                    // stage scratch
+    B_XYZ, B_BOX, B_FIDX, B_CXYZ, B_CBOX,          // run: frames and their gather
+    B_A, B_W, B_M, B_F, B_G, B_M0,                 // run: matrices
+    B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
+    B_FFT0, B_FFT1, B_FFTY, B_FFTX,
+    B_COUNT
+};
+
+}  // namespace
+
+struct cir_ctx {
+    cir_params p;
+    int natoms = 0, nmol = 0, n = 0, ld = 0;
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    DevBuf buf[B_COUNT];
+    cir_stats stats;
+    cudaEvent_t ev[8];
+    CirMaps maps;
+};
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+static bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+static int count_launch(cir_ctx *c, int k) {
+    c->stats.kernel_launches += k;
+    return CIR_OK;
+}
+
+// Device pointer for an argument: the pointer itself, or a staging buffer filled from host.
+static int stage_in(cir_ctx *c, int slot, const void *host_or_dev, size_t bytes, void **out, bool copy) {
+    if (is_device_ptr(host_or_dev)) {
+        *out = const_cast<void *>(host_or_dev);
+        return CIR_OK;
+    }
+    CK(c->buf[slot].ensure(bytes));
+    if (copy && host_or_dev) CK(cudaMemcpyAsync(c->buf[slot].p, host_or_dev, bytes, cudaMemcpyHostToDevice, c->stream));
+    *out = c->buf[slot].p;
+    return CIR_OK;
+}
+
+static int stage_out(cir_ctx *c, void *dst, const void *dev, size_t bytes) {
+    if (!dst || dst == dev) return CIR_OK;
+    CK(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return CIR_OK;
+}
+
+static bool all_finite(const float *x, size_t n) {
+    for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(x[i])) return false;
+    return true;
+}
+
+extern "C" int cir_create(const cir_params *p, int natoms, cir_ctx **out) {
+    if (!p || !out) return cir_fail(CIR_ERR_ARG, "cir_create: null pointer");
+    *out = nullptr;
+    cir_params q = *p;
+    int rc = cir_params_finalize(&q);
+    if (rc) return rc;
+    if (natoms < q.natom_mol || natoms % q.natom_mol)
+        return cir_fail(CIR_ERR_ARG, "natoms %d is not a positive multiple of natom_mol %d", natoms, q.natom_mol);
+    if (q.precision != CIR_PREC_FP32)
+        return cir_fail(CIR_ERR_ARG, "precision %d: only the plain FP32 form (CIR_PREC_FP32) is built", q.precision);
+    const int nmol = natoms / q.natom_mol;
+    const int n = nmol * q.nchrom_mol;
+    if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "%d chromophores exceed the supported %d", n, cir_eigh_max_n());
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return cir_fail(CIR_ERR_NODEVICE, "no CUDA device is available");
+    }
+    cir_ctx *c = new cir_ctx();
+    c->p = q;
+    c->natoms = natoms;
+    c->nmol = nmol;
+    c->n = n;
+    c->ld = (n + 3) & ~3;
+    cir_maps(q.map, q.ispecies, &c->maps);
+    memset(&c->stats, 0, sizeof c->stats);
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    for (int i = 0; e == cudaSuccess && i < 8; i++) e = cudaEventCreate(&c->ev[i]);
+    if (e != cudaSuccess) {
+        delete c;
+        return cir_fail(CIR_ERR_CUDA, "cir_create: %s", cudaGetErrorString(e));
+    }
+    c->stream = c->own;
+    *out = c;
+    return CIR_OK;
+}
+
+extern "C" int cir_destroy(cir_ctx *c) {
+    if (!c) return CIR_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &b : c->buf) b.release();
+    for (auto &e : c->ev) cudaEventDestroy(e);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return CIR_OK;
+}
+
+extern "C" int cir_set_stream(cir_ctx *c, void *s) {
+    if (!c) return cir_fail(CIR_ERR_ARG, "cir_set_stream: null context");
+    c->stream = s ? static_cast<cudaStream_t>(s) : c->own;
+    return CIR_OK;
+}
+
+extern "C" int cir_synchronize(cir_ctx *c) {
+    if (!c) return cir_fail(CIR_ERR_ARG, "cir_synchronize: null context");
+    CK(cudaStreamSynchronize(c->stream));
+    return CIR_OK;
+}
+
+extern "C" int cir_get_stats(cir_ctx *c, cir_stats *s) {
+    if (!c || !s) return cir_fail(CIR_ERR_ARG, "cir_get_stats: null pointer");
+    *s = c->stats;
+    return CIR_OK;
+}
+
+extern "C" int cir_reset_stats(cir_ctx *c) {
+    if (!c) return cir_fail(CIR_ERR_ARG, "cir_reset_stats: null context");
+    memset(&c->stats, 0, sizeof c->stats);
+    return CIR_OK;
+}
+
+static BuildArgs build_args(cir_ctx *c) {
+    BuildArgs a;
+    memset(&a, 0, sizeof a);
+    a.natoms = c->natoms;
+    a.natom_mol = c->p.natom_mol;
+    a.nchrom_mol = c->p.nchrom_mol;
+    a.nmol = c->nmol;
+    a.n = c->n;
+    a.ld = c->ld;
+    a.imodel = c->p.imodel;
+    a.ispecies = c->p.ispecies;
+    a.avef = c->p.avef;
+    a.maps = c->maps;
+    return a;
+}
+
+extern "C" int cir_build_hamiltonian(cir_ctx *c, int nframes, const float *xyz, const float *box, float *H,
+                                     float *eproj, float *dip, float *pol) {
+    if (!c || !xyz || !box || !H || nframes < 1) return cir_fail(CIR_ERR_ARG, "cir_build_hamiltonian: bad argument");
+    const int n = c->n;
+    const size_t nx = (size_t)nframes * c->natoms * 3;
+    if (!is_device_ptr(xyz) && !all_finite(xyz, nx)) return cir_fail(CIR_ERR_NONFINITE, "positions contain NaN or Inf");
+    if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
+    void *dx, *db, *dH, *dE = nullptr, *dD = nullptr, *dP = nullptr;
+    int rc;
+    if ((rc = stage_in(c, B_IN0, xyz, nx * 4, &dx, true))) return rc;
+    if ((rc = stage_in(c, B_IN1, box, (size_t)nframes * 12, &db, true))) return rc;
+    if ((rc = stage_in(c, B_IN2, H, (size_t)nframes * n * n * 4, &dH, false))) return rc;
+    if (eproj && (rc = stage_in(c, B_IN3, eproj, (size_t)nframes * n * 4, &dE, false))) return rc;
+    if (dip && (rc = stage_in(c, B_IN4, dip, (size_t)nframes * 3 * n * 4, &dD, false))) return rc;
+    if (pol && (rc = stage_in(c, B_IN5, pol, (size_t)nframes * 6 * n * 4, &dP, false))) return rc;
+    CK(c->buf[B_CT].ensure((size_t)nframes * CT_NROW * c->ld * 4));
+    BuildArgs a = build_args(c);
+    a.xyz = static_cast<const float *>(dx);
+    a.box = static_cast<const float *>(db);
+    a.ct = c->buf[B_CT].as<float>();
+    a.H = static_cast<float *>(dH);
+    a.ldh = n;
+    a.eproj = static_cast<float *>(dE);
+    a.dip = static_cast<float *>(dD);
+    a.pol = static_cast<float *>(dP);
+    a.ldv = n;
+    a.dip_fstride = 3LL * n;
+    a.pol_fstride = 6LL * n;
+    int launches = 0;
+    CK(cir_launch_build(a, nframes, c->stream, &launches));
+    count_launch(c, launches);
+    if ((rc = stage_out(c, H, dH, (size_t)nframes * n * n * 4))) return rc;
+    if (eproj && (rc = stage_out(c, eproj, dE, (size_t)nframes * n * 4))) return rc;
+    if (dip && (rc = stage_out(c, dip, dD, (size_t)nframes * 3 * n * 4))) return rc;
+    if (pol && (rc = stage_out(c, pol, dP, (size_t)nframes * 6 * n * 4))) return rc;
+    if (!is_device_ptr(H)) CK(cudaStreamSynchronize(c->stream));
+    return CIR_OK;
+}
+
+extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
+    if (!c || !A || !w || nmat < 1 || n < 1) return cir_fail(CIR_ERR_ARG, "cir_eigh: bad argument");
+    if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "cir_eigh: n = %d exceeds %d", n, cir_eigh_max_n());
+    // the kernel wants a leading dimension that is a multiple of 4: stage through a padded copy
+    const int ld = (n + 3) & ~3;
+    const size_t mb = (size_t)n * ld * 4;
+    CK(c->buf[B_PAD].ensure(nmat * mb));
+    CK(c->buf[B_Z].ensure(nmat * mb));
+    CK(c->buf[B_ROT].ensure(nmat * cir_eigh_rot_bytes(n)));
+    CK(c->buf[B_STATUS].ensure((size_t)nmat * 4));
+    CK(c->buf[B_SWEEPS].ensure(8));
+    CK(c->buf[B_IN1].ensure((size_t)nmat * n * 4));
+    CK(cudaMemsetAsync(c->buf[B_SWEEPS].p, 0, 8, c->stream));
+    CK(cudaMemcpy2DAsync(c->buf[B_PAD].p, (size_t)ld * 4, A, (size_t)n * 4, (size_t)n * 4, (size_t)nmat * n,
+                         cudaMemcpyDefault, c->stream));
+    EighArgs a;
+    memset(&a, 0, sizeof a);
+    a.A = c->buf[B_PAD].as<float>();
+    a.W = c->buf[B_IN1].as<float>();
+    a.Z = c->buf[B_Z].as<float>();
+    a.rot = c->buf[B_ROT].as<float2>();
+    a.mstride = (long long)n * ld;
+    a.wstride = n;
+    a.n = n;
+    a.ld = ld;
+    a.status = c->buf[B_STATUS].as<int>();
+    a.sweeps = c->buf[B_SWEEPS].as<unsigned long long>();
+    a.nchrom_mol = c->p.nchrom_mol;
+    int launches = 0;
+    CK(cir_launch_eigh(a, nmat, c->stream, &launches));
+    count_launch(c, launches);
+    CK(cudaMemcpy2DAsync(A, (size_t)n * 4, c->buf[B_PAD].p, (size_t)ld * 4, (size_t)n * 4, (size_t)nmat * n,
+                         cudaMemcpyDefault, c->stream));
+    CK(cudaMemcpyAsync(w, a.W, (size_t)nmat * n * 4, cudaMemcpyDefault, c->stream));
+    std::vector<int> st(nmat);
+    unsigned long long sweeps = 0;
+    CK(cudaMemcpyAsync(st.data(), a.status, (size_t)nmat * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&sweeps, a.sweeps, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->stats.eig_sweeps += (long long)sweeps;
+    for (int i = 0; i < nmat; i++)
+        if (st[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached on matrix %d", i);
+    return CIR_OK;
+}
+
+// F <- V diag(exp(+i w dt/hbar)) V^T F for `nprop` chains; all pointers on the device.
+static int propagate_dev(cir_ctx *c, int nprop, int n, const float *V, int ldv, long long sV, const float *w,
+                         int wstride, float dt, float *F, int ldf, long long sF, float *G) {
+    GemmArgs g1;
+    memset(&g1, 0, sizeof g1);
+    g1.A = V; g1.lda = ldv; g1.sA = sV; g1.a_colmajor = false;      // V^T as a row-major view of V
+    g1.B = F; g1.ldb = ldf; g1.sB = sF;
+    g1.C = G; g1.ldc = ldf; g1.sC = sF;
+    g1.M = n; g1.N = 2 * n; g1.K = n;
+    g1.epilogue = 1; g1.w = w; g1.wstride = wstride;
+    g1.dt_over_hbar = (float)(dt / CIR_HBAR);
+    GemmArgs g2 = g1;
+    g2.A = V; g2.a_colmajor = true;                                   // V itself
+    g2.B = G; g2.C = F; g2.epilogue = 0;
+    int launches = 0;
+    CK(cir_launch_gemm(g1, nprop, c->stream, &launches));
+    CK(cir_launch_gemm(g2, nprop, c->stream, &launches));
+    count_launch(c, launches);
+    return CIR_OK;
+}
+
+extern "C" int cir_propagate(cir_ctx *c, int nprop, int n, const float *V, const float *w, float dt, float *F) {
+    if (!c || !V || !w || !F || nprop < 1 || n < 1) return cir_fail(CIR_ERR_ARG, "cir_propagate: bad argument");
+    const size_t mb = (size_t)n * n * 4;
+    void *dV, *dW, *dF;
+    int rc;
+    if ((rc = stage_in(c, B_IN0, V, nprop * mb, &dV, true))) return rc;
+    if ((rc = stage_in(c, B_IN1, w, (size_t)nprop * n * 4, &dW, true))) return rc;
+    if ((rc = stage_in(c, B_IN2, F, nprop * mb * 2, &dF, true))) return rc;
+    CK(c->buf[B_SCR].ensure(nprop * mb * 2));
+    rc = propagate_dev(c, nprop, n, static_cast<float *>(dV), n, (long long)n * n, static_cast<float *>(dW), n, dt,
+                       static_cast<float *>(dF), 2 * n, 2LL * n * n, c->buf[B_SCR].as<float>());
+    if (rc) return rc;
+    if ((rc = stage_out(c, F, dF, nprop * mb * 2))) return rc;
+    if (!is_device_ptr(F)) CK(cudaStreamSynchronize(c->stream));
+    return CIR_OK;
+}
+
+extern "C" int cir_tcf_terms(cir_ctx *c, int n, const float *F, const float *dip0, const float *pol0,
+                             const float *dip, const float *pol, double *out) {
+    if (!c || !F || !dip0 || !pol0 || !dip || !pol || !out || n < 1) return cir_fail(CIR_ERR_ARG, "cir_tcf_terms: bad argument");
+    void *dF, *d0, *p0, *d1, *p1;
+    int rc;
+    if ((rc = stage_in(c, B_IN0, F, (size_t)n * n * 8, &dF, true))) return rc;
+    if ((rc = stage_in(c, B_IN1, dip0, (size_t)3 * n * 4, &d0, true))) return rc;
+    if ((rc = stage_in(c, B_IN2, pol0, (size_t)6 * n * 4, &p0, true))) return rc;
+    if ((rc = stage_in(c, B_IN3, dip, (size_t)3 * n * 4, &d1, true))) return rc;
+    if ((rc = stage_in(c, B_IN4, pol, (size_t)6 * n * 4, &p1, true))) return rc;
+    CK(c->buf[B_SCR].ensure((size_t)18 * n * 4 + 64));
+    float *m = c->buf[B_SCR].as<float>();
+    CK(cudaMemcpyAsync(m, d0, (size_t)3 * n * 4, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(m + 3 * n, p0, (size_t)6 * n * 4, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(m + 9 * n, d1, (size_t)3 * n * 4, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(m + 12 * n, p1, (size_t)6 * n * 4, cudaMemcpyDeviceToDevice, c->stream));
+    double *acc = reinterpret_cast<double *>(m + 18 * n);
+    CK(cudaMemsetAsync(acc, 0, 48, c->stream));
+    TcfArgs t;
+    memset(&t, 0, sizeof t);
+    t.F = static_cast<float *>(dF);
+    t.m0 = m;
+    t.mt = m + 9 * n;
+    t.out = acc;
+    t.n = n;
+    t.ldf = 2 * n;
+    t.ldv = n;
+    int launches = 0;
+    CK(cir_launch_tcf(t, 1, c->stream, &launches));
+    count_launch(c, launches);
+    CK(cudaMemcpyAsync(out, acc, 48, is_device_ptr(out) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+    if (!is_device_ptr(out)) CK(cudaStreamSynchronize(c->stream));
+    return CIR_OK;
+}
+
+extern "C" int cir_spectral_density(cir_ctx *c, int n, const float *V, const float *w, const float *dip, float *Sw) {
+    if (!c || !V || !w || !dip || !Sw || n < 1) return cir_fail(CIR_ERR_ARG, "cir_spectral_density: bad argument");
+    const int nomega = cir_nomega(&c->p);
+    void *dV, *dW, *dD;
+    int rc;
+    if ((rc = stage_in(c, B_IN0, V, (size_t)n * n * 4, &dV, true))) return rc;
+    if ((rc = stage_in(c, B_IN1, w, (size_t)n * 4, &dW, true))) return rc;
+    if ((rc = stage_in(c, B_IN2, dip, (size_t)3 * n * 4, &dD, true))) return rc;
+    CK(c->buf[B_SCR].ensure((size_t)n * 4 + (size_t)nomega * 8 + 64));
+    float *mu2 = c->buf[B_SCR].as<float>();
+    double *acc = reinterpret_cast<double *>(c->buf[B_SCR].as<char>() + (((size_t)n * 4 + 15) & ~(size_t)15));
+    CK(cudaMemsetAsync(acc, 0, (size_t)nomega * 8, c->stream));
+    int launches = 0;
+    CK(cir_launch_spectral(static_cast<float *>(dV), n, static_cast<float *>(dW), static_cast<float *>(dD), n, n, mu2,
+                           acc, nomega, c->p.omegaStart, c->p.omegaStep, c->p.t1, c->p.avef, c->stream, &launches));
+    count_launch(c, launches);
+    std::vector<double> h(nomega);
+    CK(cudaMemcpyAsync(h.data(), acc, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (is_device_ptr(Sw)) {
+        std::vector<float> cur(nomega);
+        CK(cudaMemcpy(cur.data(), Sw, (size_t)nomega * 4, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nomega; i++) cur[i] += (float)h[i];
+        CK(cudaMemcpy(Sw, cur.data(), (size_t)nomega * 4, cudaMemcpyHostToDevice));
+    } else {
+        for (int i = 0; i < nomega; i++) Sw[i] += (float)h[i];
+    }
+    return CIR_OK;
+}
+
+// Frequency axis and intensity rows of the three lineshape files (calcIR.cu:890-919);
+// y = C2R transform (length n) of one damped TCF.
+static int lineshape_rows(const cir_params *p, const double *y, float *omega, float *inten) {
+    const int n = p->ntcfpoints + p->nzeros;
+    const float factor = (float)(2 * CIR_PI * CIR_HBAR / (p->dt * (float)n));
+    const float norm = factor * (float)n;
+    int cnt = 0;
+    for (int i = n / 2; i < n; i++) {
+        const float freq = -1 * (i - p->ntcfpoints - p->nzeros) * factor + p->avef;
+        if (freq <= (float)p->omegaStop) {
+            if (omega) omega[cnt] = freq;
+            if (inten) inten[cnt] = (float)y[i] / norm;
+            cnt++;
+        }
+    }
+    for (int i = 0; i < p->ntcfpoints + p->nzeros / 2; i++) {
+        const float freq = -1 * i * factor + p->avef;
+        if (freq >= (float)p->omegaStart) {
+            if (omega) omega[cnt] = freq;
+            if (inten) inten[cnt] = (float)y[i] / norm;
+            cnt++;
+        }
+    }
+    return cnt;
+}
+
+static int c2r_dev(cir_ctx *c, const double *tcf_host, std::vector<double> &y) {
+    const int n = c->p.ntcfpoints + c->p.nzeros;
+    const int nx = c->p.ntcfpoints;
+    CK(c->buf[B_FFT0].ensure((size_t)n * 16));
+    CK(c->buf[B_FFT1].ensure((size_t)n * 16));
+    CK(c->buf[B_FFTY].ensure((size_t)n * 8));
+    CK(c->buf[B_FFTX].ensure((size_t)nx * 16));
+    CK(cudaMemcpyAsync(c->buf[B_FFTX].p, tcf_host, (size_t)nx * 16, cudaMemcpyHostToDevice, c->stream));
+    int launches = 0;
+    CK(cir_launch_c2r(c->buf[B_FFTX].as<double>(), nx, n, c->buf[B_FFT0].as<double>(), c->buf[B_FFT1].as<double>(),
+                      c->buf[B_FFTY].as<double>(), c->stream, &launches));
+    count_launch(c, launches);
+    y.resize(n);
+    CK(cudaMemcpyAsync(y.data(), c->buf[B_FFTY].p, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CIR_OK;
+}
+
+extern "C" int cir_lineshape(cir_ctx *c, const double *tcf, float *omega, float *intensity, int *nls) {
+    if (!c || !tcf) return cir_fail(CIR_ERR_ARG, "cir_lineshape: bad argument");
+    std::vector<double> y;
+    int rc = c2r_dev(c, tcf, y);
+    if (rc) return rc;
+    const int cnt = lineshape_rows(&c->p, y.data(), omega, intensity);
+    if (nls) *nls = cnt;
+    return CIR_OK;
+}
+
+namespace {
+__global__ void k_gather_frames(const float *xyz, const float *box, const int *fidx, int natoms, int s_count,
+                                int kn, int K, int k0, float *oxyz, float *obox) {
+    const int b = blockIdx.y;                     // b = s*kn + (k - k0)
+    const int s = b / kn, k = k0 + b % kn;
+    const int f = fidx[s * K + k];
+    const float *src = xyz + (size_t)f * natoms * 3;
+    float *dst = oxyz + (size_t)b * natoms * 3;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < natoms * 3; i += gridDim.x * blockDim.x) dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x < 3) obox[3 * b + threadIdx.x] = box[3 * f + threadIdx.x];
+}
+__global__ void k_copy_m0(const float *m, long long sm_origin, int rows_ld, float *m0) {
+    const int s = blockIdx.y;
+    const float *src = m + (size_t)s * sm_origin;
+    float *dst = m0 + (size_t)s * 9 * rows_ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 9 * rows_ld; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+}  // namespace
+
+extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *box, const int *frame_of_step,
+                       cir_result *r) {
+    if (!c || !xyz || !box || !r || nframes < 1) return cir_fail(CIR_ERR_ARG, "cir_run: bad argument");
+    const cir_params &p = c->p;
+    const int S = p.nsamples, K = p.ntcfpoints, n = c->n, ld = c->ld;
+    const int nomega = cir_nomega(&p);
+    const long long steps = (long long)S * K;
+    std::vector<int> fidx(steps);
+    if (frame_of_step) {
+        for (long long i = 0; i < steps; i++) {
+            if (frame_of_step[i] < 0 || frame_of_step[i] >= nframes)
+                return cir_fail(CIR_ERR_ARG, "frame_of_step[%lld] = %d outside [0, %d)", i, frame_of_step[i], nframes);
+            fidx[i] = frame_of_step[i];
+        }
+    } else {
+        if (nframes != steps) return cir_fail(CIR_ERR_ARG, "cir_run: %d frames for %lld frame-steps", nframes, steps);
+        for (long long i = 0; i < steps; i++) fidx[i] = (int)i;
+    }
+    const size_t nx = (size_t)nframes * c->natoms * 3;
+    const bool host_in = !is_device_ptr(xyz);
+    if (host_in && !all_finite(xyz, nx)) return cir_fail(CIR_ERR_NONFINITE, "positions contain NaN or Inf");
+    if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
+
+    // chunk: kn consecutive steps of all S origins per batch
+    const size_t per_step = (size_t)2 * n * ld * 4 + cir_eigh_rot_bytes(n) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
+    size_t budget = (size_t)24 << 30;
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
+    int kn = (int)std::max<size_t>(1, budget / (per_step * S));
+    if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / S);
+    kn = std::min(kn, K);
+
+    void *dxyz, *dbox;
+    int rc;
+    if ((rc = stage_in(c, B_XYZ, xyz, nx * 4, &dxyz, true))) return rc;
+    if ((rc = stage_in(c, B_BOX, box, (size_t)nframes * 12, &dbox, true))) return rc;
+    CK(c->buf[B_FIDX].ensure((size_t)steps * 4));
+    CK(cudaMemcpyAsync(c->buf[B_FIDX].p, fidx.data(), (size_t)steps * 4, cudaMemcpyHostToDevice, c->stream));
+    const int nb = S * kn;
+    const long long mstride = (long long)n * ld;
+    CK(c->buf[B_CXYZ].ensure((size_t)nb * c->natoms * 12));
+    CK(c->buf[B_CBOX].ensure((size_t)nb * 12));
+    CK(c->buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
+    CK(c->buf[B_A].ensure((size_t)nb * mstride * 4));
+    CK(c->buf[B_Z].ensure((size_t)nb * mstride * 4));
+    CK(c->buf[B_ROT].ensure((size_t)nb * cir_eigh_rot_bytes(n)));
+    CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
+    CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
+    CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
+    CK(c->buf[B_F].ensure((size_t)S * n * 2 * ld * 4));
+    CK(c->buf[B_G].ensure((size_t)S * n * 2 * ld * 4));
+    CK(c->buf[B_M0].ensure((size_t)S * 9 * ld * 4));
+    CK(c->buf[B_TCF].ensure((size_t)steps * 6 * 8));
+    CK(c->buf[B_HCNT].ensure((size_t)nomega * 8));
+    CK(c->buf[B_HIPR].ensure((size_t)nomega * 8));
+    CK(c->buf[B_HMIPR].ensure((size_t)nomega * 8));
+    CK(c->buf[B_OOR].ensure(8));
+    CK(c->buf[B_SWEEPS].ensure(8));
+    CK(c->buf[B_SW].ensure((size_t)nomega * 8));
+    CK(c->buf[B_MU2].ensure((size_t)ld * 4));
+    CK(cudaMemsetAsync(c->buf[B_TCF].p, 0, (size_t)steps * 48, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_HCNT].p, 0, (size_t)nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_HIPR].p, 0, (size_t)nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_HMIPR].p, 0, (size_t)nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_OOR].p, 0, 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_SWEEPS].p, 0, 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_SW].p, 0, (size_t)nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_STATUS].p, 0, (size_t)nb * 4, c->stream));
+
+    float *A = c->buf[B_A].as<float>(), *W = c->buf[B_W].as<float>(), *M = c->buf[B_M].as<float>();
+    float *F = c->buf[B_F].as<float>(), *G = c->buf[B_G].as<float>(), *M0 = c->buf[B_M0].as<float>();
+    double *tcf = c->buf[B_TCF].as<double>();
+    int launches = 0;
+    cudaEvent_t *ev = c->ev;
+    CK(cudaEventRecord(ev[0], c->stream));
+    for (int k0 = 0; k0 < K; k0 += kn) {
+        const int kc = std::min(kn, K - k0);
+        const int nbc = S * kc;
+        CK(cudaEventRecord(ev[1], c->stream));
+        k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(static_cast<float *>(dxyz), static_cast<float *>(dbox),
+                                                             c->buf[B_FIDX].as<int>(), c->natoms, S, kc, K, k0,
+                                                             c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
+        CK(cudaGetLastError());
+        launches++;
+        BuildArgs a = build_args(c);
+        a.xyz = c->buf[B_CXYZ].as<float>();
+        a.box = c->buf[B_CBOX].as<float>();
+        a.ct = c->buf[B_CT].as<float>();
+        a.H = A;
+        a.ldh = ld;
+        a.dip = M;                    // frame b: M + b*9*ld, rows 0..2 dipole, 3..8 polarisability
+        a.pol = M + 3 * ld;
+        a.ldv = ld;
+        a.dip_fstride = 9LL * ld;
+        a.pol_fstride = 9LL * ld;
+        CK(cir_launch_build(a, nbc, c->stream, &launches));
+        CK(cudaEventRecord(ev[2], c->stream));
+        EighArgs e;
+        memset(&e, 0, sizeof e);
+        e.A = A;
+        e.W = W;
+        e.Z = c->buf[B_Z].as<float>();
+        e.rot = c->buf[B_ROT].as<float2>();
+        e.mstride = mstride;
+        e.wstride = ld;
+        e.n = n;
+        e.ld = ld;
+        e.status = c->buf[B_STATUS].as<int>();
+        e.sweeps = c->buf[B_SWEEPS].as<unsigned long long>();
+        e.hist_count = c->buf[B_HCNT].as<unsigned long long>();
+        e.hist_ipr = c->buf[B_HIPR].as<double>();
+        e.hist_mipr = c->buf[B_HMIPR].as<double>();
+        e.out_of_range = c->buf[B_OOR].as<unsigned long long>();
+        e.nomega = nomega;
+        e.omegaStep = p.omegaStep;
+        e.nchrom_mol = p.nchrom_mol;
+        e.avef = p.avef;
+        e.omegaStart = p.omegaStart;
+        CK(cir_launch_eigh(e, nbc, c->stream, &launches));
+        CK(cudaEventRecord(ev[3], c->stream));
+        if (k0 == 0) {
+            // spectral density at step 0 of every origin (calcIR.cu:456-482)
+            for (int s = 0; s < S; s++) {
+                const size_t b = (size_t)s * kc;
+                CK(cir_launch_spectral(A + b * mstride, ld, W + b * ld, M + b * 9 * ld, ld, n, c->buf[B_MU2].as<float>(),
+                                       c->buf[B_SW].as<double>(), nomega, p.omegaStart, p.omegaStep, p.t1, p.avef,
+                                       c->stream, &launches));
+            }
+            // F = I and the t = 0 vectors (calcIR.cu:577-594)
+            CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, S, c->stream, &launches));
+            k_copy_m0<<<dim3(4, S), 256, 0, c->stream>>>(M, (long long)kc * 9 * ld, ld, M0);
+            CK(cudaGetLastError());
+            launches++;
+        }
+        for (int k = k0; k < k0 + kc; k++) {
+            const int kk = k - k0;
+            if (k > 0) {   // F <- V_k exp(i L_k dt/hbar) V_k^T F for every origin (calcIR.cu:596-617)
+                int rc2 = propagate_dev(c, S, n, A + (size_t)kk * mstride, ld, (long long)kc * mstride, W + (size_t)kk * ld,
+                                        kc * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G);
+                if (rc2) return rc2;
+            }
+            TcfArgs t;
+            memset(&t, 0, sizeof t);
+            t.F = F;
+            t.sF = (long long)n * 2 * ld;
+            t.m0 = M0;
+            t.sm0 = 9LL * ld;
+            t.mt = M + (size_t)kk * 9 * ld;
+            t.smt = (long long)kc * 9 * ld;
+            t.out = tcf + (size_t)k * 6;
+            t.sout = (long long)K * 6;
+            t.n = n;
+            t.ldf = 2 * ld;
+            t.ldv = ld;
+            CK(cir_launch_tcf(t, S, c->stream, &launches));
+        }
+        CK(cudaEventRecord(ev[4], c->stream));
+        CK(cudaEventSynchronize(ev[4]));
+        float x;
+        cudaEventElapsedTime(&x, ev[1], ev[2]);
+        c->stats.ms_build += x;
+        cudaEventElapsedTime(&x, ev[2], ev[3]);
+        c->stats.ms_eig += x;
+        cudaEventElapsedTime(&x, ev[3], ev[4]);
+        c->stats.ms_prop += x;
+    }
+    CK(cudaEventRecord(ev[7], c->stream));
+    CK(cudaEventSynchronize(ev[7]));
+    float ms_total = 0;
+    cudaEventElapsedTime(&ms_total, ev[0], ev[7]);
+    count_launch(c, launches);
+    c->stats.frame_steps += steps;
+
+    // ---------------- finishing steps (calcIR.cu:772-839) ----------------
+    std::vector<double> htcf((size_t)steps * 6), hipr(nomega), hmipr(nomega), hsw(nomega);
+    std::vector<unsigned long long> hcnt(nomega);
+    std::vector<int> hst(nb);
+    unsigned long long oor = 0, sweeps = 0;
+    CK(cudaMemcpyAsync(htcf.data(), tcf, (size_t)steps * 48, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hcnt.data(), c->buf[B_HCNT].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hipr.data(), c->buf[B_HIPR].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hmipr.data(), c->buf[B_HMIPR].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hsw.data(), c->buf[B_SW].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hst.data(), c->buf[B_STATUS].p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&oor, c->buf[B_OOR].p, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&sweeps, c->buf[B_SWEEPS].p, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->stats.eig_sweeps += (long long)sweeps;
+    for (int i = 0; i < nb; i++)
+        if (hst[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached");
+
+    // sum over origins, T1 damping and 1/nsamples (calcIR.cu:777-782, 798-802, 815-819)
+    std::vector<double> damped[3];
+    for (int q = 0; q < 3; q++) damped[q].assign((size_t)2 * K, 0.0);
+    for (int k = 0; k < K; k++) {
+        double sum[6] = {0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < S; s++)
+            for (int q = 0; q < 6; q++) sum[q] += htcf[((size_t)s * K + k) * 6 + q];
+        const double dcy = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
+        for (int q = 0; q < 3; q++) {
+            damped[q][2 * k] = sum[2 * q] * dcy;
+            damped[q][2 * k + 1] = sum[2 * q + 1] * dcy;
+        }
+    }
+    double *outs[3] = {r->tcf_ir, r->tcf_vv, r->tcf_vh};
+    for (int q = 0; q < 3; q++)
+        if (outs[q]) memcpy(outs[q], damped[q].data(), (size_t)2 * K * 8);
+    // spectral density and frequency distributions (calcIR.cu:831-839)
+    const float norm = (float)(n * S * K);
+    for (int i = 0; i < nomega; i++) {
+        if (r->omega) r->omega[i] = (float)(p.omegaStart + p.omegaStep * i);
+        if (r->sw) r->sw[i] = (float)(hsw[i] / S);
+        const float pw = (float)((double)hcnt[i] / p.omegaStep) / norm;
+        if (r->pw) r->pw[i] = pw;
+        if (r->rw) r->rw[i] = ((float)(hipr[i] / p.omegaStep) / norm) / pw;
+        if (r->rmw) r->rmw[i] = ((float)(hmipr[i] / p.omegaStep) / norm) / pw;
+    }
+    // lineshapes (calcIR.cu:786-827, 890-919)
+    float *lsv[3] = {r->ls_ir, r->ls_vv, r->ls_vh};
+    int nls = 0;
+    for (int q = 0; q < 3; q++) {
+        std::vector<double> y;
+        int rc3 = c2r_dev(c, damped[q].data(), y);
+        if (rc3) return rc3;
+        nls = lineshape_rows(&p, y.data(), q == 0 ? r->ls_omega : nullptr, lsv[q]);
+    }
+    r->nls = nls;
+    r->bins_out_of_range = (long long)oor;
+    r->frame_steps_per_s = ms_total > 0 ? steps / (ms_total * 1e-3) : 0.0;
+    return CIR_OK;
+}

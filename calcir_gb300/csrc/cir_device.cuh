@@ -1,0 +1,118 @@
+// Device-side helpers and the kernel entry points shared by the .cu files.
+#ifndef CIR_DEVICE_CUH_
+#define CIR_DEVICE_CUH_
+
+#include <cuda_runtime.h>
+#include "cir_internal.h"
+
+// minImage (calcIR.cu:1459-1463): dx - L*round(dx/L), round half away from zero.
+__device__ __forceinline__ float cir_mi(float dx, float L) { return dx - L * roundf(dx / L); }
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per-chromophore quantities produced by the field kernel, struct-of-arrays per frame:
+// row r of a frame's [CT_NROW][ld] block.
+enum {
+    CT_E = 0,     // field projection (a.u.)
+    CT_W,         // map frequency omega (cm^-1)
+    CT_X,         // map x
+    CT_P,         // map p
+    CT_MUP,       // map mu'
+    CT_UX, CT_UY, CT_UZ,   // OH unit vector
+    CT_TX, CT_TY, CT_TZ,   // transition dipole position, wrapped by minImage
+    CT_NROW
+};
+
+struct BuildArgs {
+    const float *xyz;     // [nframes][natoms][3]
+    const float *box;     // [nframes][3]
+    float *ct;            // [nframes][CT_NROW][ld] chromophore table
+    float *H;             // [nframes][n][ldh]
+    float *eproj;         // [nframes][n]  or null
+    float *dip;           // frame f: rows x,y,z at dip + f*dip_fstride + {0,1,2}*ldv, or null
+    float *pol;           // frame f: rows xx,yy,zz,xy,yz,zx at pol + f*pol_fstride + r*ldv, or null
+    long long dip_fstride, pol_fstride;
+    int natoms, natom_mol, nchrom_mol, nmol, n;
+    int ld;               // leading dimension of the chromophore table rows
+    int ldh;              // row stride of H
+    int ldv;              // row stride of dip/pol
+    int imodel, ispecies;
+    float avef;
+    CirMaps maps;
+};
+
+struct EighArgs {
+    float *A;             // [nmat] matrices, column j of matrix m at A + m*mstride + j*ld
+    float *W;             // [nmat][wstride] eigenvalues
+    float *Z;             // scratch, same shape as A
+    float2 *rot;          // scratch, cir_eigh_rot_bytes(n) per matrix
+    long long mstride;
+    int wstride;
+    int n, ld;
+    int *status;          // [nmat] 0 ok, 1 sweep cap reached
+    unsigned long long *sweeps;   // accumulated QR sweeps (may be null)
+    // frequency distribution (calcIR.cu:493-538); hist_count == null disables it
+    unsigned long long *hist_count;
+    double *hist_ipr, *hist_mipr;
+    unsigned long long *out_of_range;
+    int nomega, omegaStep, nchrom_mol;
+    float avef, omegaStart;
+};
+
+// kernel launchers (return cudaError_t of the launch)
+cudaError_t cir_launch_build(const BuildArgs &a, int nframes, cudaStream_t s, int *launches);
+cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
+size_t cir_eigh_smem_bytes(int n);
+size_t cir_eigh_rot_bytes(int n);
+int cir_eigh_max_n();
+
+// batched SIMT FP32 GEMM, C = A * B (row-major B, C); A row- or column-major.
+// epilogue 1: rotate column pairs (2q, 2q+1) of row i by exp(+i w[i] dt/hbar).
+struct GemmArgs {
+    const float *A, *B;
+    float *C;
+    int M, N, K;
+    int lda, ldb, ldc;
+    long long sA, sB, sC;  // batch strides (elements)
+    bool a_colmajor;
+    int epilogue;          // 0 none, 1 phase rotation
+    const float *w;        // [batch][wstride] for epilogue 1
+    int wstride;
+    float dt_over_hbar;
+};
+cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches);
+
+// TCF terms: out[b][6] += (IR, VV, VH) for batch element b
+struct TcfArgs {
+    const float *F;        // [batch] complex row-major, row stride ldf floats (2 per element)
+    long long sF;
+    const float *m0;       // [batch][9][ldv] dip0 (3) then pol0 (6)
+    const float *mt;       // [batch][9][ldv]
+    long long sm0, smt;
+    double *out;           // [batch][6]
+    long long sout;
+    int n, ldf, ldv;
+};
+cudaError_t cir_launch_tcf(const TcfArgs &t, int batch, cudaStream_t s, int *launches);
+
+// spectral density of one frame: Sw[nomega] += ...
+cudaError_t cir_launch_spectral(const float *V, int ld, const float *w, const float *dip, int ldv, int n,
+                                float *mu2_scratch, double *Sw, int nomega, float omegaStart, int omegaStep,
+                                float t1, float avef, cudaStream_t s, int *launches);
+
+// unnormalised inverse real DFT (cuFFT C2R convention) of X[0..n/2] (complex double)
+// into y[n], by a mixed-radix Stockham FFT in double precision
+cudaError_t cir_launch_c2r(const double *X, int nx, int n, double *work0, double *work1, double *y,
+                           cudaStream_t s, int *launches);
+
+// F = I for nprop complex matrices
+cudaError_t cir_launch_identity(float *F, int n, int ldf, long long sF, int batch, cudaStream_t s, int *launches);
+
+#endif
