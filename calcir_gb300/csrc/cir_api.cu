@@ -49,7 +49,7 @@ enum {
     B_XYZ, B_BOX, B_FIDX, B_CXYZ, B_CBOX,          // run: frames and their gather
     B_A, B_W, B_M, B_F, B_G, B_M0,                 // run: matrices
     B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
-    B_FFT0, B_FFT1, B_FFTY, B_FFTX,
+    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE,
     B_COUNT
 };
 
@@ -80,6 +80,32 @@ static bool is_device_ptr(const void *p) {
         return false;
     }
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// CIR_EIGH_PROFILE=1: per-phase wall time of the eigensolver blocks, printed to stderr
+static bool eigh_profiling() {
+    const char *v = getenv("CIR_EIGH_PROFILE");
+    return v && v[0] == '1';
+}
+
+static void eigh_profile_report(const unsigned long long *dev, int nmat, cudaStream_t s) {
+    std::vector<unsigned long long> h((size_t)nmat * 8);
+    if (cudaMemcpyAsync(h.data(), dev, h.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) return;
+    cudaStreamSynchronize(s);
+    double sum[4] = {0, 0, 0, 0}, chase = 0, apply = 0, nrot = 0;
+    unsigned long long t0 = ~0ull, t1 = 0;
+    for (int m = 0; m < nmat; m++) {
+        for (int q = 0; q < 4; q++) sum[q] += (double)(h[m * 8 + q + 1] - h[m * 8 + q]);
+        t0 = std::min(t0, h[m * 8]);
+        t1 = std::max(t1, h[m * 8 + 4]);
+        chase += (double)h[m * 8 + 5];
+        apply += (double)h[m * 8 + 6];
+        nrot += (double)h[m * 8 + 7];
+    }
+    fprintf(stderr, "eigh profile: %d matrices, span %.3f ms; mean per block (ms): tridiag %.3f formQ %.3f qr %.3f "
+                    "(chase %.3f, apply %.3f, %.0f rotations) sort %.3f\n",
+            nmat, (t1 - t0) * 1e-6, sum[0] / nmat * 1e-6, sum[1] / nmat * 1e-6, sum[2] / nmat * 1e-6,
+            chase / nmat * 1e-6, apply / nmat * 1e-6, nrot / nmat, sum[3] / nmat * 1e-6);
 }
 
 static int count_launch(cir_ctx *c, int k) {
@@ -247,6 +273,7 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     CK(c->buf[B_PAD].ensure(nmat * mb));
     CK(c->buf[B_Z].ensure(nmat * mb));
     CK(c->buf[B_ROT].ensure(nmat * cir_eigh_rot_bytes(n)));
+    CK(c->buf[B_DE].ensure(nmat * cir_eigh_de_bytes(ld)));
     CK(c->buf[B_STATUS].ensure((size_t)nmat * 4));
     CK(c->buf[B_SWEEPS].ensure(8));
     CK(c->buf[B_IN1].ensure((size_t)nmat * n * 4));
@@ -259,6 +286,7 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     a.W = c->buf[B_IN1].as<float>();
     a.Z = c->buf[B_Z].as<float>();
     a.rot = c->buf[B_ROT].as<float2>();
+    a.DE = c->buf[B_DE].as<float>();
     a.mstride = (long long)n * ld;
     a.wstride = n;
     a.n = n;
@@ -266,9 +294,15 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     a.status = c->buf[B_STATUS].as<int>();
     a.sweeps = c->buf[B_SWEEPS].as<unsigned long long>();
     a.nchrom_mol = c->p.nchrom_mol;
+    if (eigh_profiling()) {
+        CK(c->buf[B_PROF].ensure((size_t)nmat * 8 * 8));
+        CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * 8 * 8, c->stream));
+        a.phase_ns = c->buf[B_PROF].as<unsigned long long>();
+    }
     int launches = 0;
     CK(cir_launch_eigh(a, nmat, c->stream, &launches));
     count_launch(c, launches);
+    if (a.phase_ns) eigh_profile_report(a.phase_ns, nmat, c->stream);
     CK(cudaMemcpy2DAsync(A, (size_t)n * 4, c->buf[B_PAD].p, (size_t)ld * 4, (size_t)n * 4, (size_t)nmat * n,
                          cudaMemcpyDefault, c->stream));
     CK(cudaMemcpyAsync(w, a.W, (size_t)nmat * n * 4, cudaMemcpyDefault, c->stream));
@@ -483,7 +517,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
 
     // chunk: kn consecutive steps of all S origins per batch
-    const size_t per_step = (size_t)2 * n * ld * 4 + cir_eigh_rot_bytes(n) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
+    const size_t per_step = (size_t)2 * n * ld * 4 + cir_eigh_rot_bytes(n) + cir_eigh_de_bytes(ld) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
     size_t budget = (size_t)24 << 30;
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
@@ -505,6 +539,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     CK(c->buf[B_A].ensure((size_t)nb * mstride * 4));
     CK(c->buf[B_Z].ensure((size_t)nb * mstride * 4));
     CK(c->buf[B_ROT].ensure((size_t)nb * cir_eigh_rot_bytes(n)));
+    CK(c->buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
     CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
     CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
     CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
@@ -562,6 +597,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         e.W = W;
         e.Z = c->buf[B_Z].as<float>();
         e.rot = c->buf[B_ROT].as<float2>();
+        e.DE = c->buf[B_DE].as<float>();
         e.mstride = mstride;
         e.wstride = ld;
         e.n = n;
@@ -577,7 +613,13 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         e.nchrom_mol = p.nchrom_mol;
         e.avef = p.avef;
         e.omegaStart = p.omegaStart;
+        if (eigh_profiling()) {
+            CK(c->buf[B_PROF].ensure((size_t)nbc * 8 * 8));
+            CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nbc * 8 * 8, c->stream));
+            e.phase_ns = c->buf[B_PROF].as<unsigned long long>();
+        }
         CK(cir_launch_eigh(e, nbc, c->stream, &launches));
+        if (e.phase_ns) eigh_profile_report(e.phase_ns, nbc, c->stream);
         CK(cudaEventRecord(ev[3], c->stream));
         if (k0 == 0) {
             // spectral density at step 0 of every origin (calcIR.cu:456-482)

@@ -53,6 +53,7 @@ struct EighArgs {
     float *W;             // [nmat][wstride] eigenvalues
     float *Z;             // scratch, same shape as A
     float2 *rot;          // scratch, cir_eigh_rot_bytes(n) per matrix
+    float *DE;            // scratch, cir_eigh_de_bytes(ld) per matrix (tridiagonal d, e)
     long long mstride;
     int wstride;
     int n, ld;
@@ -64,13 +65,14 @@ struct EighArgs {
     unsigned long long *out_of_range;
     int nomega, omegaStep, nchrom_mol;
     float avef, omegaStart;
+    unsigned long long *phase_ns;   // optional [nmat][5] %globaltimer at phase boundaries
 };
 
 // kernel launchers (return cudaError_t of the launch)
 cudaError_t cir_launch_build(const BuildArgs &a, int nframes, cudaStream_t s, int *launches);
 cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
-size_t cir_eigh_smem_bytes(int n);
 size_t cir_eigh_rot_bytes(int n);
+size_t cir_eigh_de_bytes(int ld);
 int cir_eigh_max_n();
 
 // batched SIMT FP32 GEMM, C = A * B (row-major B, C); A row- or column-major.

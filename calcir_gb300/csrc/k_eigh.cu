@@ -1,6 +1,8 @@
 // Batched symmetric eigensolver for the exciton Hamiltonians (replaces magma_ssyevd_gpu,
-// calcIR.cu:420-448).  One thread block solves one matrix; a launch solves a batch of
-// frames, so the SMs work on independent frames at once.
+// calcIR.cu:420-448).  Two kernels, each with one thread block per matrix, so the SMs
+// work on independent frames at once: k_eigh_tq (phases 1-2, 256 threads) and k_eigh_qr
+// (phases 3-4, 128 threads: one chasing warp and three applying warps, four blocks per SM
+// so that four bulge chases overlap on every SM).
 //
 //  1. Householder tridiagonalisation Q^T H Q = T (reflectors stored below the
 //     subdiagonal, as LAPACK sytd2).  The rank-2 update of step k-1 and the
@@ -10,8 +12,9 @@
 //     of EIG_NB reflectors staged in shared memory; each warp keeps one column segment of
 //     Z in registers while a block is applied.
 //  3. Implicit symmetric QR on T with the Wilkinson shift (Golub & Van Loan, Alg. 8.3.2).
-//     Lane 0 of warp 0 chases the bulges of a group of EIG_KS sweeps while the other
-//     warps apply the previous group to the rows of Z.  A group is applied as a
+//     Lane 0 of warp 0 chases the bulges of a group of EIG_KS sweeps (the bulge state is
+//     carried in registers) while the other warps apply the previous group to the rows
+//     of Z.  A group is applied as a
 //     wavefront: sweep s trails sweep s-1 by one column, so each row keeps a window of
 //     EIG_KS+1 columns in registers and reads and writes every column once per group
 //     instead of once per sweep.
@@ -26,9 +29,26 @@
 
 namespace {
 
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 constexpr int EIG_NB = 8;      // reflectors per block in phase 2
 constexpr int EIG_KS = 16;     // QR sweeps per wavefront group in phase 3
 constexpr int EIG_W = EIG_KS + 1;
+constexpr int QR_PREFETCH = 4;  // Z columns loaded ahead of the wavefront in phase 3
+
+size_t tq_smem_bytes(int n) {
+    const size_t n4 = (size_t)((n + 3) & ~3);
+    return sizeof(float) * (3 * n4 + EIG_NB * n4 + 64);
+}
+
+size_t qr_smem_bytes(int n) {
+    const size_t n4 = (size_t)((n + 3) & ~3);
+    return sizeof(float) * 3 * n4 + sizeof(int) * (4 * EIG_KS + 8);
+}
 
 template <int NT>
 __device__ __forceinline__ float block_sum(float v, float *red) {
@@ -53,12 +73,16 @@ __device__ __forceinline__ bool negligible(float e, float d0, float d1, float ti
 struct Chaser {
     int cm, nsweep, status, cap;
     float tiny;
+    long long nrot;
 };
 
 // One implicit QR sweep with the Wilkinson shift on the trailing unreduced block of
-// (d, e); its rotations go to rot[l..cm-1] (rotation i acts on columns i, i+1).
+// (d, e); rotation i (acting on columns i, i+1) goes to rot[(i + s_slot) * EIG_KS].
 // Returns false when T is diagonal or the sweep cap is reached.
-__device__ bool qr_sweep(Chaser &ch, float *d, float *e, float2 *rot, int *lo, int *hi) {
+// rot points at slot s of a time-major group buffer: rotation i of this sweep is stored at
+// rot[(i + s) * EIG_KS], so the EIG_KS rotations applied at one wavefront step share one
+// 128-byte line.
+__device__ bool qr_sweep(Chaser &ch, float *d, float *e, float2 *rot, int s_slot, int *lo, int *hi) {
     int cm = ch.cm;
     while (cm > 0 && negligible(e[cm - 1], d[cm - 1], d[cm], ch.tiny)) { e[cm - 1] = 0.f; cm--; }
     ch.cm = cm;
@@ -70,106 +94,133 @@ __device__ bool qr_sweep(Chaser &ch, float *d, float *e, float2 *rot, int *lo, i
     const float bb = e[cm - 1];
     const float den = t + copysignf(sqrtf(t * t + bb * bb), t);
     const float mu = d[cm] - (den != 0.f ? bb * bb / den : 0.f);
+    // bulge state in registers: dk = current d[k], ek = current e[k]; dk1/ek1 are the
+    // untouched d[k+1], e[k+1], loaded one iteration ahead
     float x = d[l] - mu, z = e[l];
+    float dk = d[l], ek = e[l];
+    float dk1 = d[l + 1], ek1 = (l + 1 < cm) ? e[l + 1] : 0.f;
     for (int k = l; k < cm; k++) {
-        const float r = sqrtf(x * x + z * z);
-        float c = 1.f, s = 0.f;
-        if (r > 0.f) { c = x / r; s = z / r; }
-        if (k > l) e[k - 1] = r;
-        const float a0 = d[k], a1 = d[k + 1], be = e[k];
-        const float g = s * (a0 - a1) - 2.f * c * be;
-        d[k] = a0 - s * g;
-        d[k + 1] = a1 + s * g;
-        e[k] = c * s * (a1 - a0) + (c * c - s * s) * be;
-        if (k + 1 < cm) {
-            const float b2 = e[k + 1];
-            z = s * b2;
-            e[k + 1] = c * b2;
-            x = e[k];
+        const float dk2 = (k + 2 <= cm) ? d[k + 2] : 0.f;
+        const float ek2 = (k + 2 < cm) ? e[k + 2] : 0.f;
+        const float r2 = x * x + z * z;
+        float c = 1.f, s = 0.f, r = 0.f;
+        if (r2 >= 1e-30f) {
+            // reciprocal square root refined by one FMA-based Newton step (as accurate as a
+            // correctly rounded rsqrt for the orthogonality of the rotations)
+            const float i0 = rsqrtf(r2);
+            const float res = fmaf(-(r2 * i0), i0, 1.0f);
+            const float inv = fmaf(0.5f * i0, res, i0);
+            c = x * inv;
+            s = z * inv;
+            r = r2 * inv;
+        } else if (r2 > 0.f) {
+            r = sqrtf(r2);
+            c = x / r;
+            s = z / r;
         }
-        rot[k] = make_float2(c, s);
+        if (k > l) e[k - 1] = r;
+        const float g = s * (dk - dk1) - 2.f * c * ek;
+        d[k] = dk - s * g;
+        const float dk1n = dk1 + s * g;
+        const float ekn = c * s * (dk1 - dk) + (c * c - s * s) * ek;
+        e[k] = ekn;
+        float ek_next = 0.f;
+        if (k + 1 < cm) {
+            z = s * ek1;
+            ek_next = c * ek1;
+            x = ekn;
+        }
+        rot[(size_t)(k + s_slot) * EIG_KS] = make_float2(c, s);
+        dk = dk1n;
+        ek = ek_next;
+        dk1 = dk2;
+        ek1 = ek2;
     }
+    d[cm] = dk;
     *lo = l;
     *hi = cm;
     ch.nsweep++;
+    ch.nrot += cm - l;
     return true;
 }
 
-// Apply a group of `cnt` sweeps (rotations rot[s*n + i], i in [lo[s], hi[s])) to rows
-// ra and rb of Z as a wavefront (see the file comment).
-__device__ __forceinline__ void apply_group(float *Z, int ld, int ra, int rb, bool va, bool vb,
-                                            const float2 *rot, int n, const int *lo, const int *hi, int cnt) {
-    int T0 = 1 << 30, T1 = -1, cmin = 1 << 30, cmax = -1;
-    for (int s = 0; s < cnt; s++) {
-        T0 = min(T0, lo[s] + s);
-        T1 = max(T1, hi[s] - 1 + s);
-        cmin = min(cmin, lo[s]);
-        cmax = max(cmax, hi[s]);
-    }
-    if (T1 < 0) return;
-    int los[EIG_KS], his[EIG_KS];
+// Apply a group of `cnt` sweeps to R rows of Z as a wavefront.  Rotation i of sweep s
+// lives at rot[(i + s) * EIG_KS + s]; every other slot of the group buffer holds the
+// identity rotation (c = 1, s = 0), so the EIG_KS rotations of step tau are one 128-byte
+// line rot[tau * EIG_KS ..] and are applied without predicates.  At step tau, sweep s
+// applies its rotation i = tau - s.  Each row keeps the columns tau-EIG_KS+1 .. tau+1 in
+// registers w[0..EIG_KS] (slot j holds column tau-EIG_KS+1+j); rotation (s, tau-s) acts
+// on slots EIG_KS-1-s and EIG_KS-s and the window shifts by one slot per step, so every
+// column is read and written once per group.  Slots EIG_KS+1 .. EIG_KS+P hold columns
+// loaded P steps ahead.  row[j] < 0 marks an unused row slot.
+template <int R, int P>
+__device__ __forceinline__ void apply_group(float *Z, int ld, const int (&row)[R], const float2 *rot,
+                                            int T0, int T1, int cmin, int cmax) {
+    constexpr int S = EIG_W + P;   // window slots
+    float w[R][S];
+    // columns T0-EIG_KS+1 .. T0+P into slots 0 .. EIG_KS-1+P
     #pragma unroll
-    for (int s = 0; s < EIG_KS; s++) {
-        los[s] = s < cnt ? lo[s] : 0;
-        his[s] = s < cnt ? hi[s] : 0;
-    }
-    float wa[EIG_W], wb[EIG_W];
-    const int tb = (T0 / EIG_W) * EIG_W;
-    #pragma unroll
-    for (int v = 1; v <= EIG_KS; v++) {
-        const int c = tb - EIG_KS + v;
+    for (int v = 0; v < EIG_KS + P; v++) {
+        const int c = T0 - EIG_KS + 1 + v;
         const bool ok = c >= cmin && c <= cmax;
-        wa[(v + 1) % EIG_W] = (ok && va) ? Z[(size_t)c * ld + ra] : 0.f;
-        wb[(v + 1) % EIG_W] = (ok && vb) ? Z[(size_t)c * ld + rb] : 0.f;
-    }
-    int tc = tb;
-    for (; tc <= T1; tc += EIG_W) {
         #pragma unroll
-        for (int u = 0; u < EIG_W; u++) {
-            const int tau = tc + u;
-            {
-                const int c = tau + 1;
-                if (c >= cmin && c <= cmax) {
-                    if (va) wa[(u + 1) % EIG_W] = Z[(size_t)c * ld + ra];
-                    if (vb) wb[(u + 1) % EIG_W] = Z[(size_t)c * ld + rb];
-                }
-            }
+        for (int j = 0; j < R; j++) w[j][v] = (ok && row[j] >= 0) ? __ldcg(Z + (size_t)c * ld + row[j]) : 0.f;
+    }
+    float4 nxt[EIG_KS / 2];
+    #pragma unroll
+    for (int q = 0; q < EIG_KS / 2; q++) nxt[q] = reinterpret_cast<const float4 *>(rot + (size_t)T0 * EIG_KS)[q];
+    for (int tau = T0; tau <= T1; tau++) {
+        float4 cur[EIG_KS / 2];
+        #pragma unroll
+        for (int q = 0; q < EIG_KS / 2; q++) cur[q] = nxt[q];
+        if (tau < T1) {
             #pragma unroll
-            for (int s = 0; s < EIG_KS; s++) {
-                const int i = tau - s;
-                if (i >= los[s] && i < his[s]) {
-                    const float2 cs = rot[s * n + i];
-                    const int ia = (u - s + 2 * EIG_W) % EIG_W, ib = (u - s + 1 + 2 * EIG_W) % EIG_W;
-                    const float a0 = wa[ia], a1 = wa[ib];
-                    wa[ia] = cs.x * a0 + cs.y * a1;
-                    wa[ib] = cs.x * a1 - cs.y * a0;
-                    const float b0 = wb[ia], b1 = wb[ib];
-                    wb[ia] = cs.x * b0 + cs.y * b1;
-                    wb[ib] = cs.x * b1 - cs.y * b0;
-                }
-            }
-            {
-                const int c = tau - EIG_KS + 1;
-                if (c >= cmin && c <= cmax) {
-                    if (va) Z[(size_t)c * ld + ra] = wa[(u + 2) % EIG_W];
-                    if (vb) Z[(size_t)c * ld + rb] = wb[(u + 2) % EIG_W];
-                }
+            for (int q = 0; q < EIG_KS / 2; q++) nxt[q] = reinterpret_cast<const float4 *>(rot + (size_t)(tau + 1) * EIG_KS)[q];
+        }
+        {   // column tau+1+P into the last slot
+            const int c = tau + 1 + P;
+            const bool ok = c >= cmin && c <= cmax;
+            #pragma unroll
+            for (int j = 0; j < R; j++) w[j][S - 1] = (ok && row[j] >= 0) ? __ldcg(Z + (size_t)c * ld + row[j]) : 0.f;
+        }
+        #pragma unroll
+        for (int s = 0; s < EIG_KS; s++) {
+            const float cc = (s & 1) ? cur[s / 2].z : cur[s / 2].x;
+            const float ss = (s & 1) ? cur[s / 2].w : cur[s / 2].y;
+            #pragma unroll
+            for (int j = 0; j < R; j++) {
+                const float a0 = w[j][EIG_KS - 1 - s], a1 = w[j][EIG_KS - s];
+                w[j][EIG_KS - 1 - s] = cc * a0 + ss * a1;
+                w[j][EIG_KS - s] = cc * a1 - ss * a0;
             }
         }
+        {
+            const int c = tau - EIG_KS + 1;
+            if (c >= cmin && c <= cmax) {
+                #pragma unroll
+                for (int j = 0; j < R; j++)
+                    if (row[j] >= 0) __stcg(Z + (size_t)c * ld + row[j], w[j][0]);
+            }
+        }
+        #pragma unroll
+        for (int j = 0; j < R; j++)
+            #pragma unroll
+            for (int v = 0; v < S - 1; v++) w[j][v] = w[j][v + 1];
     }
-    const int tl = tc - 1;   // last time step processed, congruent to EIG_KS mod EIG_W
+    // after the last step the window holds columns T1-EIG_KS+2 .. T1+1 in slots 0..EIG_KS-1
     #pragma unroll
-    for (int v = 1; v < EIG_W; v++) {
-        const int c = tl - EIG_KS + 1 + v;
+    for (int v = 0; v < EIG_KS; v++) {
+        const int c = T1 - EIG_KS + 2 + v;
         if (c >= cmin && c <= cmax) {
-            if (va) Z[(size_t)c * ld + ra] = wa[(v + 1) % EIG_W];
-            if (vb) Z[(size_t)c * ld + rb] = wb[(v + 1) % EIG_W];
+            #pragma unroll
+            for (int j = 0; j < R; j++)
+                if (row[j] >= 0) __stcg(Z + (size_t)c * ld + row[j], w[j][v]);
         }
     }
 }
 
 template <int NT, int NMAX>
-__global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
+__global__ void __launch_bounds__(NT) k_eigh_tq(EighArgs a) {
     constexpr int RMAX = (NMAX + 31) / 32;            // rows per lane, phase 2
     constexpr int QG = (NMAX + 4 * NT - 1) / (4 * NT); // 4-row groups per thread, phase 1
     constexpr int NW = NT / 32;
@@ -178,7 +229,6 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float *A = a.A + (size_t)blockIdx.x * a.mstride;
     float *Z = a.Z + (size_t)blockIdx.x * a.mstride;
-    float2 *rotg = a.rot + (size_t)blockIdx.x * 2 * EIG_KS * n;
 
     const int n4 = (n + 3) & ~3;
     float *d = smem;             // [n4]
@@ -186,8 +236,9 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
     float *tau = e + n4;         // [n4]
     float *U = tau + n4;         // union region, EIG_NB*n4 floats (>= 4*n4)
     float *red = U + (size_t)EIG_NB * n4;   // [64]
-    int *isc = reinterpret_cast<int *>(red + 64);   // [4*EIG_KS + 8]
 
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * 8 : nullptr;
+    if (pt && tid == 0) pt[0] = globaltimer_ns();
     // ---------------- phase 1: tridiagonalisation ----------------
     {
         float *vp = U, *wp = U + n4, *vc = U + 2 * n4, *wc = U + 3 * n4;
@@ -336,6 +387,7 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
         __syncthreads();
     }
 
+    if (pt && tid == 0) pt[1] = globaltimer_ns();
     // ---------------- phase 2: Q = H_0 H_1 ... H_{n-3} into Z ----------------
     for (size_t idx = tid; idx < (size_t)n * ld; idx += NT) {
         const int j = (int)(idx / ld), i = (int)(idx % ld);
@@ -388,6 +440,35 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
         }
     }
 
+    // d and e for the QR kernel
+    for (int i = tid; i < n; i += NT) {
+        a.DE[(size_t)blockIdx.x * 2 * ld + i] = d[i];
+        a.DE[(size_t)blockIdx.x * 2 * ld + ld + i] = e[i];
+    }
+    if (pt && tid == 0) pt[2] = globaltimer_ns();
+}
+
+template <int NT, int R>
+__global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) float smem[];
+    const int n = a.n, ld = a.ld;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float *A = a.A + (size_t)blockIdx.x * a.mstride;
+    float *Z = a.Z + (size_t)blockIdx.x * a.mstride;
+    float2 *rotg = a.rot + (size_t)blockIdx.x * 2 * (n + EIG_KS) * EIG_KS;
+    const int n4 = (n + 3) & ~3;
+    float *d = smem;                                 // [n4]
+    float *e = d + n4;                               // [n4]
+    float *U = e + n4;                               // [n4] ranks
+    int *isc = reinterpret_cast<int *>(U + n4);      // [4*EIG_KS + 8]
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * 8 : nullptr;
+    for (int i = tid; i < n; i += NT) {
+        d[i] = a.DE[(size_t)blockIdx.x * 2 * ld + i];
+        e[i] = a.DE[(size_t)blockIdx.x * 2 * ld + ld + i];
+    }
+    for (int q = tid; q < 2 * (n + EIG_KS) * EIG_KS; q += NT) rotg[q] = make_float2(1.f, 0.f);
+    __syncthreads();
     // ---------------- phase 3: implicit QR on (d, e), rotations applied to Z ----------------
     {
         int *g_lo = isc;                 // [2][EIG_KS]
@@ -399,6 +480,8 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
         ch.status = 0;
         ch.cap = 30 * n;
         ch.tiny = 0.f;
+        ch.nrot = 0;
+        unsigned long long t_chase = 0, t_apply = 0;
         if (tid == 0) {
             float tn = 0.f;
             for (int i = 0; i < n; i++) tn = fmaxf(tn, fabsf(d[i]) + 2.f * fabsf(e[i]));
@@ -408,7 +491,8 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
         auto produce = [&](int b) {
             int cnt = 0;
             while (cnt < EIG_KS &&
-                   qr_sweep(ch, d, e, rotg + (size_t)(b * EIG_KS + cnt) * n, &g_lo[b * EIG_KS + cnt], &g_hi[b * EIG_KS + cnt]))
+                   qr_sweep(ch, d, e, rotg + (size_t)b * (n + EIG_KS) * EIG_KS + cnt, cnt, &g_lo[b * EIG_KS + cnt],
+                            &g_hi[b * EIG_KS + cnt]))
                 cnt++;
             g_cnt[b] = cnt;
         };
@@ -417,21 +501,40 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
         int b = 0;
         const int napp = NT - 32;
         while (g_cnt[b] > 0) {
+            const unsigned long long tg = pt ? globaltimer_ns() : 0ull;
             if (warp == 0) {
-                if (lane == 0) produce(b ^ 1);
+                if (lane == 0) {
+                    produce(b ^ 1);
+                    if (pt) t_chase += globaltimer_ns() - tg;
+                }
             } else {
                 const int t = tid - 32;
-                const float2 *rb = rotg + (size_t)b * EIG_KS * n;
-                for (int r0 = 0; r0 < n; r0 += 2 * napp) {
-                    const int ra = r0 + t, rb2 = r0 + napp + t;
-                    if (ra >= n) break;
-                    apply_group(Z, ld, ra, rb2 < n ? rb2 : ra, true, rb2 < n, rb, n, g_lo + b * EIG_KS,
-                                g_hi + b * EIG_KS, g_cnt[b]);
+                float2 *rb = rotg + (size_t)b * (n + EIG_KS) * EIG_KS;
+                int T0 = 1 << 30, T1 = -1, cmin = 1 << 30, cmax = -1;
+                for (int s = 0; s < g_cnt[b]; s++) {
+                    T0 = min(T0, g_lo[b * EIG_KS + s] + s);
+                    T1 = max(T1, g_hi[b * EIG_KS + s] - 1 + s);
+                    cmin = min(cmin, g_lo[b * EIG_KS + s]);
+                    cmax = max(cmax, g_hi[b * EIG_KS + s]);
                 }
+                for (int r0 = 0; r0 < n; r0 += R * napp) {
+                    if (r0 + t >= n) break;
+                    int row[R];
+                    #pragma unroll
+                    for (int j = 0; j < R; j++) row[j] = (r0 + j * napp + t < n) ? r0 + j * napp + t : -1;
+                    apply_group<R, QR_PREFETCH>(Z, ld, row, rb, T0, T1, cmin, cmax);
+                }
+                // back to identity for the group after next (the __syncthreads below orders
+                // this before the chase writes into the buffer again)
+                asm volatile("bar.sync 1, %0;" ::"r"(NT - 32));
+                for (int q = T0 * EIG_KS + t; q <= T1 * EIG_KS + EIG_KS - 1; q += napp) rb[q] = make_float2(1.f, 0.f);
+                if (pt && tid == 32) t_apply += globaltimer_ns() - tg;
             }
             __syncthreads();
             b ^= 1;
         }
+        if (pt && tid == 0) { pt[5] = t_chase; pt[7] = (unsigned long long)ch.nrot; }
+        if (pt && tid == 32) pt[6] = t_apply;
         if (tid == 0) {
             if (a.status) a.status[blockIdx.x] = ch.status;
             if (a.sweeps) atomicAdd(a.sweeps, (unsigned long long)ch.nsweep);
@@ -439,6 +542,7 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
         __syncthreads();
     }
 
+    if (pt && tid == 0) pt[3] = globaltimer_ns();
     // ---------------- phase 4: ascending order, output, frequency distribution ----------------
     {
         int *rank = reinterpret_cast<int *>(U);
@@ -487,38 +591,53 @@ __global__ void __launch_bounds__(NT) k_eigh(EighArgs a) {
             }
         }
     }
+    if (pt) {
+        __syncthreads();
+        if (tid == 0) pt[4] = globaltimer_ns();
+    }
 }
 
 template <int NT, int NMAX>
-cudaError_t launch_one(const EighArgs &a, int nmat, cudaStream_t s, size_t smem) {
-    auto kern = k_eigh<NT, NMAX>;
+cudaError_t launch_tq(const EighArgs &a, int nmat, cudaStream_t s) {
+    auto kern = k_eigh_tq<NT, NMAX>;
+    const size_t smem = tq_smem_bytes(a.n);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<nmat, NT, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-}  // namespace
+constexpr int QR_THREADS = 128;
+constexpr int QR_ROWS = 3;   // rows per applying thread; 3 blocks per SM without spills
 
-size_t cir_eigh_smem_bytes(int n) {
-    const size_t n4 = (size_t)((n + 3) & ~3);
-    return sizeof(float) * (3 * n4 + EIG_NB * n4 + 64) + sizeof(int) * (4 * EIG_KS + 8);
+cudaError_t launch_qr(const EighArgs &a, int nmat, cudaStream_t s) {
+    auto kern = k_eigh_qr<QR_THREADS, QR_ROWS>;
+    const size_t smem = qr_smem_bytes(a.n);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nmat, QR_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
 }
 
-size_t cir_eigh_rot_bytes(int n) { return sizeof(float2) * 2 * EIG_KS * (size_t)n; }
+}  // namespace
+
+size_t cir_eigh_rot_bytes(int n) { return sizeof(float2) * 2 * EIG_KS * (size_t)(n + EIG_KS); }
+
+size_t cir_eigh_de_bytes(int ld) { return sizeof(float) * 2 * (size_t)ld; }
 
 int cir_eigh_max_n() { return 2048; }
 
 cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches) {
     if (a.n < 1 || a.n > cir_eigh_max_n() || nmat < 1 || (a.ld & 3) || a.ld < a.n) return cudaErrorInvalidValue;
-    if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.rot)
+    if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.rot || !a.DE)
         return cudaErrorInvalidValue;
-    const size_t smem = cir_eigh_smem_bytes(a.n);
     cudaError_t e;
-    if (a.n <= 256) e = launch_one<128, 256>(a, nmat, s, smem);
-    else if (a.n <= 512) e = launch_one<256, 512>(a, nmat, s, smem);
-    else if (a.n <= 1024) e = launch_one<256, 1024>(a, nmat, s, smem);
-    else e = launch_one<256, 2048>(a, nmat, s, smem);
-    if (launches) *launches += 1;
+    if (a.n <= 256) e = launch_tq<128, 256>(a, nmat, s);
+    else if (a.n <= 512) e = launch_tq<256, 512>(a, nmat, s);
+    else if (a.n <= 1024) e = launch_tq<256, 1024>(a, nmat, s);
+    else e = launch_tq<256, 2048>(a, nmat, s);
+    if (e != cudaSuccess) return e;
+    e = launch_qr(a, nmat, s);
+    if (launches) *launches += 2;
     return e;
 }
