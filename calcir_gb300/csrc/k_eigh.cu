@@ -26,6 +26,8 @@
 // The leading dimension must be a multiple of 4 and A 16-byte aligned.
 #include "cir_device.cuh"
 #include <float.h>
+#include <cstring>
+#include <mutex>
 
 namespace {
 
@@ -640,4 +642,107 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     e = launch_qr(a, nmat, s);
     if (launches) *launches += 2;
     return e;
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free entry point.  Some callers cannot allocate device memory: a simulation
+// engine that calls this per frame from inside its own time step owns the GPU memory
+// budget, and cudaMalloc/cudaFree synchronise the whole device and may fail in the middle
+// of a run.  cir_eigh_noalloc takes the caller's device buffers for A and w and keeps all
+// of its scratch (the eigenvector workspace, the QR rotation groups, the tridiagonal and
+// the per-matrix status) in one statically sized device array that the library holds
+// for as long as it is loaded.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(8) << 20;   // 8 MiB on every device that loads the library
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // device address of g_noalloc_scratch, per device
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_stream) {
+    if (nmat < 1 || n < 1 || n > cir_eigh_max_n() || !A || !w)
+        return cir_fail(CIR_ERR_ARG, "cir_eigh_noalloc: need nmat >= 1, 1 <= n <= %d and device buffers A, w",
+                        cir_eigh_max_n());
+    cudaPointerAttributes pa, pw;
+    if (cudaPointerGetAttributes(&pa, A) != cudaSuccess || cudaPointerGetAttributes(&pw, w) != cudaSuccess) {
+        cudaGetLastError();
+        return cir_fail(CIR_ERR_ARG, "cir_eigh_noalloc: A and w must be device pointers");
+    }
+    if (pa.type != cudaMemoryTypeDevice || pw.type != cudaMemoryTypeDevice)
+        return cir_fail(CIR_ERR_ARG, "cir_eigh_noalloc: A and w must be device pointers");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "cir_eigh_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cir_fail(CIR_ERR_ARG, "cir_eigh_noalloc: device %d unsupported", dev);
+    unsigned char *scratch = nullptr;
+    {
+        // one-time set-up per device, with that device current: the array's device address
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess)
+                return cir_fail(CIR_ERR_CUDA, "cir_eigh_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    }
+    const int ld = (n + 3) & ~3;
+    const bool pad = (ld != n) || (reinterpret_cast<uintptr_t>(A) & 15);
+    const size_t mat = (size_t)n * ld * sizeof(float);
+    const size_t need = align256(nmat * mat)                                   // Z
+                        + align256(nmat * cir_eigh_rot_bytes(n))               // rotation groups
+                        + align256(nmat * cir_eigh_de_bytes(ld))               // d, e
+                        + align256((size_t)nmat * sizeof(int))                 // status
+                        + (pad ? align256(nmat * mat) : 0);                    // 16-byte aligned copy of A
+    if (need > NOALLOC_SCRATCH_BYTES)
+        return cir_fail(CIR_ERR_ARG,
+                        "cir_eigh_noalloc: %d matrices of order %d need %zu bytes of scratch; the allocation-free "
+                        "scratch holds %zu bytes (call it with fewer matrices at a time)",
+                        nmat, n, need, NOALLOC_SCRATCH_BYTES);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    unsigned char *q = scratch;
+    EighArgs a;
+    memset(&a, 0, sizeof a);
+    a.Z = reinterpret_cast<float *>(q); q += align256(nmat * mat);
+    a.rot = reinterpret_cast<float2 *>(q); q += align256(nmat * cir_eigh_rot_bytes(n));
+    a.DE = reinterpret_cast<float *>(q); q += align256(nmat * cir_eigh_de_bytes(ld));
+    a.status = reinterpret_cast<int *>(q); q += align256((size_t)nmat * sizeof(int));
+    a.A = pad ? reinterpret_cast<float *>(q) : A;
+    a.W = w;
+    a.mstride = (long long)n * ld;
+    a.wstride = n;
+    a.n = n;
+    a.ld = ld;
+    a.nchrom_mol = 2;
+    if (pad) {
+        e = cudaMemcpy2DAsync(a.A, (size_t)ld * 4, A, (size_t)n * 4, (size_t)n * 4, (size_t)nmat * n,
+                              cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "cir_eigh_noalloc: %s", cudaGetErrorString(e));
+    }
+    e = cir_launch_eigh(a, nmat, s, nullptr);
+    if (e != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "cir_eigh_noalloc: launch: %s", cudaGetErrorString(e));
+    if (pad) {
+        e = cudaMemcpy2DAsync(A, (size_t)n * 4, a.A, (size_t)ld * 4, (size_t)n * 4, (size_t)nmat * n,
+                              cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "cir_eigh_noalloc: %s", cudaGetErrorString(e));
+    }
+    // the per-matrix convergence flags, read back through a small stack buffer
+    int st[256];
+    for (int m0 = 0; m0 < nmat; m0 += 256) {
+        const int cnt = nmat - m0 < 256 ? nmat - m0 : 256;
+        e = cudaMemcpyAsync(st, a.status + m0, (size_t)cnt * sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "cir_eigh_noalloc: %s", cudaGetErrorString(e));
+        for (int i = 0; i < cnt; i++)
+            if (st[i]) return cir_fail(CIR_ERR_NOCONVERGE, "cir_eigh_noalloc: sweep cap reached on matrix %d", m0 + i);
+    }
+    return CIR_OK;
 }

@@ -171,6 +171,23 @@ int cir_build_hamiltonian(cir_ctx *c, int nframes, const float *xyz, const float
  * Replaces magma_ssyevd_gpu + the w copy (calcIR.cu:420-448). */
 int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w);
 
+/* The batched eigensolver of cir_eigh for callers that cannot allocate device memory
+ * (no counterpart in the reference).  A host application that owns the GPU memory
+ * budget -- for example a simulation engine calling this per frame from inside its own
+ * time step -- cannot let a library call cudaMalloc/cudaFree, which synchronise the
+ * device and can fail mid-run.  This entry point allocates nothing: A [nmat][n][n] and
+ * w [nmat][n] are the caller's DEVICE buffers (same meaning as cir_eigh), and all scratch
+ * lives in one 8 MiB device array that every GPU which loads the library holds until the
+ * process exits.  Requests whose scratch exceeds 8 MiB (more than one matrix of order
+ * 1024, seven of order 512 or 25 of order 256 per call) are rejected with CIR_ERR_ARG;
+ * split the batch instead.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the one array and
+ * every call overwrites it, so calls that overlap on the GPU (different streams or host
+ * threads without ordering) race.  The call is issued on cuda_stream (NULL: the default
+ * stream) and returns after that stream has finished it. */
+int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_stream);
+
 /* One propagation step of nprop independent chains: F <- V diag(exp(+i w dt/hbar)) V^T F,
  * V [nprop][n][n] eigenvectors as returned by cir_eigh, w [nprop][n], F [nprop][n][n]
  * complex.  Replaces Pinit + 3 x magma_cgemm + magma_ccopy (calcIR.cu:596-617). */
