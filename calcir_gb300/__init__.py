@@ -196,7 +196,7 @@ class Engine:
         n = V.shape[-1]
         Vc = np.ascontiguousarray(np.swapaxes(V, 1, 2))        # column j contiguous
         w = np.ascontiguousarray(np.asarray(w, np.float32).reshape(-1, n))
-        Fi = np.array(F, np.complex64, copy=True).reshape(-1, n, n)   # the library updates F in place
+        Fi = np.array(F, np.complex64, copy=True, order="C").reshape(-1, n, n)   # updated in place by the library
         Fr = Fi.view(np.float32)
         check(self.lib.cir_propagate(self.h, V.shape[0], n, ptr(Vc), ptr(w), C.c_float(dt), ptr(Fr)))
         out = Fr.view(np.complex64)
