@@ -1,0 +1,78 @@
+"""Small drivers for profiling single stages of the CUDA path (run under ncu or with
+CIR_EIGH_PROFILE=1 for the eigensolver's per-phase timers).
+
+    python -m calcir_gb300.profile eigh --nmol 512 --batch 152
+    python -m calcir_gb300.profile prop --n 1024 --nprop 10
+    python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 250
+
+Every stage goes through the C ABI (libcalcir.so)."""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+import calcir_gb300 as cg
+
+
+def eigh(nmol: int, batches: list[int], seed: int = 3) -> None:
+    xyz, box = cg.synth_trajectory(nmol, 8, seed=seed)
+    p = cg.default_params(model="tip4p2005", species="H2O", avef=3415.0)
+    with cg.Engine(p, xyz.shape[1]) as eng:
+        H, _, _, _ = eng.build_hamiltonian(xyz, box)
+        for nb in batches:
+            A = np.ascontiguousarray(np.broadcast_to(H[np.arange(nb) % 8], (nb,) + H.shape[1:]))
+            t = time.time()
+            eng.eigh(A)
+            dt = time.time() - t
+            print(f"eigh N={H.shape[-1]} batch {nb}: {dt:.3f} s wall ({nb / dt:.1f} matrices/s incl. copies)", flush=True)
+
+
+def prop(n: int, nprop: int, precision: str = "fp32") -> None:
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((n, n)).astype(np.float32)
+    A = (a + a.T) * np.float32(300 / np.sqrt(8 * n))
+    with cg.Engine(cg.default_params(species="H2O", precision=precision), 8) as eng:
+        w, V = eng.eigh(A)
+        F = np.broadcast_to(np.eye(n, dtype=np.complex64), (nprop, n, n))
+        out = eng.propagate(np.broadcast_to(V, (nprop, n, n)), np.broadcast_to(w, (nprop, n)), 0.01, F)
+    print(f"prop N={n} x {nprop}: max |F| {np.abs(out).max():.4f}", flush=True)
+
+
+def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32") -> None:
+    p = cg.default_params(model="tip4p2005", species="H2O", ntcfpoints=ntcf, nsamples=nsamples, sampleEvery=2.0,
+                          avef=3415.0, omegaStart=1000, omegaStop=5000, omegaStep=1, precision=precision)
+    fos = cg.frame_table(p, 0.010)
+    xyz, box = cg.synth_trajectory(nmol, int(fos.max()) + 1, seed=1)
+    with cg.Engine(p, xyz.shape[1]) as eng:
+        out = eng.run(xyz, box, fos)
+        print(f"run nmol {nmol}: {out['frame_steps_per_s']:.1f} frame-steps/s", eng.stats(), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    e = sub.add_parser("eigh")
+    e.add_argument("--nmol", type=int, default=512)
+    e.add_argument("--batch", default="152")
+    pr = sub.add_parser("prop")
+    pr.add_argument("--n", type=int, default=1024)
+    pr.add_argument("--nprop", type=int, default=10)
+    pr.add_argument("--precision", default="fp32")
+    r = sub.add_parser("run")
+    r.add_argument("--nmol", type=int, default=512)
+    r.add_argument("--nsamples", type=int, default=10)
+    r.add_argument("--ntcf", type=int, default=250)
+    r.add_argument("--precision", default="fp32")
+    a = ap.parse_args()
+    if a.cmd == "eigh":
+        eigh(a.nmol, [int(x) for x in a.batch.split(",")])
+    elif a.cmd == "prop":
+        prop(a.n, a.nprop, a.precision)
+    else:
+        run(a.nmol, a.nsamples, a.ntcf, a.precision)
+
+
+if __name__ == "__main__":
+    main()
