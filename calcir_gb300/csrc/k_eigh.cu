@@ -221,8 +221,8 @@ __device__ __forceinline__ void apply_group(float *Z, int ld, const int (&row)[R
     }
 }
 
-template <int NT, int NMAX>
-__global__ void __launch_bounds__(NT) k_eigh_tq(EighArgs a) {
+template <int NT, int NMAX, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     constexpr int RMAX = (NMAX + 31) / 32;            // rows per lane, phase 2
     constexpr int QG = (NMAX + 4 * NT - 1) / (4 * NT); // 4-row groups per thread, phase 1
     constexpr int NW = NT / 32;
@@ -599,9 +599,11 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
     }
 }
 
-template <int NT, int NMAX>
+// MINB: resident blocks per SM the register budget is fitted to (3 while the spill stays
+// negligible; the order-2048 variant keeps 2 because its Q phase would spill).
+template <int NT, int NMAX, int MINB>
 cudaError_t launch_tq(const EighArgs &a, int nmat, cudaStream_t s) {
-    auto kern = k_eigh_tq<NT, NMAX>;
+    auto kern = k_eigh_tq<NT, NMAX, MINB>;
     const size_t smem = tq_smem_bytes(a.n);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -634,10 +636,10 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.rot || !a.DE)
         return cudaErrorInvalidValue;
     cudaError_t e;
-    if (a.n <= 256) e = launch_tq<128, 256>(a, nmat, s);
-    else if (a.n <= 512) e = launch_tq<256, 512>(a, nmat, s);
-    else if (a.n <= 1024) e = launch_tq<256, 1024>(a, nmat, s);
-    else e = launch_tq<256, 2048>(a, nmat, s);
+    if (a.n <= 256) e = launch_tq<128, 256, 4>(a, nmat, s);
+    else if (a.n <= 512) e = launch_tq<256, 512, 3>(a, nmat, s);
+    else if (a.n <= 1024) e = launch_tq<256, 1024, 3>(a, nmat, s);
+    else e = launch_tq<256, 2048, 2>(a, nmat, s);
     if (e != cudaSuccess) return e;
     e = launch_qr(a, nmat, s);
     if (launches) *launches += 2;
