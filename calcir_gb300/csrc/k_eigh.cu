@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
 }
 
 // MINB: resident blocks per SM the register budget is fitted to (3 while the spill stays
-// negligible; the order-2048 variant is not constrained because its Q phase would spill).
+// negligible; the order-2048 variant is fitted to 2 blocks).
 template <int NT, int NMAX, int MINB>
 cudaError_t launch_tq(const EighArgs &a, int nmat, cudaStream_t s) {
     auto kern = k_eigh_tq<NT, NMAX, MINB>;
@@ -639,7 +639,7 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     if (a.n <= 256) e = launch_tq<128, 256, 4>(a, nmat, s);
     else if (a.n <= 512) e = launch_tq<256, 512, 3>(a, nmat, s);
     else if (a.n <= 1024) e = launch_tq<256, 1024, 3>(a, nmat, s);
-    else e = launch_tq<256, 2048, 1>(a, nmat, s);
+    else e = launch_tq<256, 2048, 2>(a, nmat, s);
     if (e != cudaSuccess) return e;
     e = launch_qr(a, nmat, s);
     if (launches) *launches += 2;
