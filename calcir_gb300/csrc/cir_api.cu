@@ -49,7 +49,7 @@ enum {
     B_XYZ, B_BOX, B_FIDX, B_CXYZ, B_CBOX,          // run: frames and their gather
     B_A, B_W, B_M, B_F, B_G, B_M0,                 // run: matrices
     B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
-    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE,
+    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR,
     B_COUNT
 };
 
@@ -145,8 +145,8 @@ extern "C" int cir_create(const cir_params *p, int natoms, cir_ctx **out) {
     if (rc) return rc;
     if (natoms < q.natom_mol || natoms % q.natom_mol)
         return cir_fail(CIR_ERR_ARG, "natoms %d is not a positive multiple of natom_mol %d", natoms, q.natom_mol);
-    if (q.precision != CIR_PREC_FP32)
-        return cir_fail(CIR_ERR_ARG, "precision %d: only the plain FP32 form (CIR_PREC_FP32) is built", q.precision);
+    if (q.precision != CIR_PREC_FP32 && q.precision != CIR_PREC_TF32)
+        return cir_fail(CIR_ERR_ARG, "precision %d is not built (CIR_PREC_FP32 and CIR_PREC_TF32 are)", q.precision);
     const int nmol = natoms / q.natom_mol;
     const int n = nmol * q.nchrom_mol;
     if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "%d chromophores exceed the supported %d", n, cir_eigh_max_n());
@@ -171,7 +171,23 @@ extern "C" int cir_create(const cir_params *p, int natoms, cir_ctx **out) {
         return cir_fail(CIR_ERR_CUDA, "cir_create: %s", cudaGetErrorString(e));
     }
     c->stream = c->own;
+    if (c->buf[B_ERR].ensure(sizeof(int)) != cudaSuccess || cudaMemset(c->buf[B_ERR].p, 0, sizeof(int)) != cudaSuccess) {
+        cir_destroy(c);
+        return cir_fail(CIR_ERR_CUDA, "cir_create: cannot allocate the error flag");
+    }
     *out = c;
+    return CIR_OK;
+}
+
+// The tensor-core kernels set the context's error flag when a bounded wait gives up.
+static int check_kernel_flag(cir_ctx *c) {
+    int flag = 0;
+    CK(cudaMemcpyAsync(&flag, c->buf[B_ERR].p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (flag) {
+        cudaMemsetAsync(c->buf[B_ERR].p, 0, sizeof(int), c->stream);
+        return cir_fail(CIR_ERR_CUDA, "a tensor-core kernel timed out waiting on its pipeline");
+    }
     return CIR_OK;
 }
 
@@ -332,8 +348,15 @@ static int propagate_dev(cir_ctx *c, int nprop, int n, const float *V, int ldv, 
     g2.A = V; g2.a_colmajor = true;                                   // V itself
     g2.B = G; g2.C = F; g2.epilogue = 0;
     int launches = 0;
-    CK(cir_launch_gemm(g1, nprop, c->stream, &launches));
-    CK(cir_launch_gemm(g2, nprop, c->stream, &launches));
+    if (c->p.precision == CIR_PREC_FP32) {
+        CK(cir_launch_gemm(g1, nprop, c->stream, &launches));
+        CK(cir_launch_gemm(g2, nprop, c->stream, &launches));
+    } else {
+        CK(c->buf[B_ERR].ensure(sizeof(int)));
+        g1.err = g2.err = c->buf[B_ERR].as<int>();
+        CK(cir_launch_tc_gemm(g1, nprop, c->p.precision, c->stream, &launches));
+        CK(cir_launch_tc_gemm(g2, nprop, c->p.precision, c->stream, &launches));
+    }
     count_launch(c, launches);
     return CIR_OK;
 }
@@ -352,6 +375,7 @@ extern "C" int cir_propagate(cir_ctx *c, int nprop, int n, const float *V, const
     if (rc) return rc;
     if ((rc = stage_out(c, F, dF, nprop * mb * 2))) return rc;
     if (!is_device_ptr(F)) CK(cudaStreamSynchronize(c->stream));
+    if (c->p.precision != CIR_PREC_FP32 && (rc = check_kernel_flag(c))) return rc;
     return CIR_OK;
 }
 
@@ -691,6 +715,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     c->stats.eig_sweeps += (long long)sweeps;
     for (int i = 0; i < nb; i++)
         if (hst[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached");
+    if (p.precision != CIR_PREC_FP32 && (rc = check_kernel_flag(c))) return rc;
 
     // sum over origins, T1 damping and 1/nsamples (calcIR.cu:777-782, 798-802, 815-819)
     std::vector<double> damped[3];

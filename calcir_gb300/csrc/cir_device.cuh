@@ -88,8 +88,12 @@ struct GemmArgs {
     const float *w;        // [batch][wstride] for epilogue 1
     int wstride;
     float dt_over_hbar;
+    int *err;              // tensor-core kernels: set to 1 when a bounded wait gives up
 };
 cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches);
+// the same product on the tensor cores (tcgen05), precision CIR_PREC_TF32
+cudaError_t cir_launch_tc_gemm(const GemmArgs &g, int batch, int precision, cudaStream_t s, int *launches);
+size_t cir_tc_gemm_smem_bytes();
 
 // TCF terms: out[b][6] += (IR, VV, VH) for batch element b
 struct TcfArgs {

@@ -266,3 +266,23 @@ def test_run_full_size_against_oracle(lib):
         out = eng.run(xyz, box, fos)
     ref = O.run(prm, xyz, [box] * len(xyz), fos)
     _compare_run(out, ref, prm, SPEC_TOL, "full512")
+
+
+@pytest.mark.parametrize("n", [200, 1024])
+def test_propagate_tensor_core_tf32(lib, n):
+    """The tcgen05 TF32 propagation against the FP64 statement of the same step; TF32
+    inputs carry 11 significant bits, so the bound is 2e-3 relative."""
+    rng = np.random.default_rng(n + 7)
+    nprop, dt = 2, 0.010
+    A = np.stack([_sym(rng, n) for _ in range(nprop)])
+    F = (rng.standard_normal((nprop, n, n)) + 1j * rng.standard_normal((nprop, n, n))).astype(np.complex64)
+    with lib.Engine(lib.default_params(species="H2O", precision="tf32"), 8) as eng:
+        w, V = eng.eigh(A)
+        out = eng.propagate(V, w, np.float32(dt), F)
+    for m in range(nprop):
+        V64 = V[m].astype(np.float64)
+        ph = np.exp(1j * w[m].astype(np.float64) * np.float32(dt) / HBAR)
+        ref = (V64 * ph[None, :]) @ (V64.T @ F[m].astype(np.complex128))
+        err = O.rel_l2(out[m], ref)
+        assert err < 2e-3, err
+        assert err > 1e-7, "tensor-core path produced FP32-exact output: is it running?"
