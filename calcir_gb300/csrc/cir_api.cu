@@ -145,8 +145,7 @@ extern "C" int cir_create(const cir_params *p, int natoms, cir_ctx **out) {
     if (rc) return rc;
     if (natoms < q.natom_mol || natoms % q.natom_mol)
         return cir_fail(CIR_ERR_ARG, "natoms %d is not a positive multiple of natom_mol %d", natoms, q.natom_mol);
-    if (q.precision != CIR_PREC_FP32 && q.precision != CIR_PREC_TF32)
-        return cir_fail(CIR_ERR_ARG, "precision %d is not built (CIR_PREC_FP32 and CIR_PREC_TF32 are)", q.precision);
+
     const int nmol = natoms / q.natom_mol;
     const int n = nmol * q.nchrom_mol;
     if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "%d chromophores exceed the supported %d", n, cir_eigh_max_n());

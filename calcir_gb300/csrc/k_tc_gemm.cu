@@ -5,11 +5,11 @@
 //
 // One CTA computes a 128 x 128 tile with 128 threads:
 //   * all threads stage 32-deep K slices of A and B from global memory into shared
-//     memory, rounded to TF32 (round to nearest), in the non-swizzled K-major
-//     core-matrix layout: core matrix (r/8, k/4) at (r/8)*SBO + (k/4)*LBO, 8 rows of 16
-//     bytes inside.  LBO = 144 and SBO = 1168 bytes are padded so the 16-byte stores
-//     of a warp spread over all bank groups;
-//   * one thread issues the tcgen05.mma instructions (K = 8 each) of a stage and
+//     memory, converted to the operand type (TF32 rounded to nearest, or BF16 hi/lo
+//     pairs), in the non-swizzled K-major core-matrix layout: core matrix (r/8, k/CK)
+//     at (r/8)*SBO + (k/CK)*LBO, 8 rows of 16 bytes inside.  The strides are padded
+//     (TF32: 144/1168 bytes, BF16: 128/528) so a warp's stores spread over the banks;
+//   * one thread issues the tcgen05.mma instructions of a stage and
 //     signals their completion to the stage's mbarrier with tcgen05.commit; two stages
 //     let the loads of the next slice overlap the MMAs of the current one;
 //   * the accumulator lives in 128 TMEM columns; each warp reads its 32 lanes with
@@ -26,10 +26,22 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 32;   // tile; TK in elements per stage (TF32)
-constexpr int LBO = 144, SBO = 1168;          // bytes, see above
-constexpr int TILE_BYTES = (TM / 8) * SBO;    // 18688 bytes per operand tile
+constexpr int TM = 128, TN = 128, TK = 32;   // tile; TK elements of K per stage
 constexpr int NTHREADS = 128;
+
+// Shared-memory tile layouts (K-major, no swizzle): core matrix (r/8, k/CK) at
+// (r/8)*SBO + (k/CK)*LBO, rows of 16 bytes inside; CK = elements per 16 bytes.
+// TF32: 8 core matrices along K per stage; BF16: 4, stored as separate hi and lo tiles.
+template <int MODE> struct Cfg;
+template <> struct Cfg<CIR_PREC_TF32> {
+    static constexpr int LBO = 144, SBO = 1168, CK = 4, KSTEP = 8, PARTS = 1;
+    static constexpr uint32_t FMT = 2;   // TF32
+};
+template <> struct Cfg<CIR_PREC_BF16X3> {
+    static constexpr int LBO = 128, SBO = 528, CK = 8, KSTEP = 16, PARTS = 2;
+    static constexpr uint32_t FMT = 1;   // BF16
+};
+template <int MODE> __host__ __device__ constexpr int tile_bytes() { return (TM / 8) * Cfg<MODE>::SBO; }
 constexpr long long WAIT_LIMIT = 1ll << 24;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -56,11 +68,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
+template <int MODE>
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     // start address >> 4, leading (K) byte offset >> 4, stride (M/N) byte offset >> 4,
     // fixed field 0b001 at bit 46, no swizzle
-    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(LBO >> 4) << 16) | ((uint64_t)(SBO >> 4) << 32) |
-           (1ull << 46);
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(Cfg<MODE>::LBO >> 4) << 16) |
+           ((uint64_t)(Cfg<MODE>::SBO >> 4) << 32) | (1ull << 46);
 }
 
 // instruction descriptor: D f32, A/B format, K-major A and B, N = 128, M = 128
@@ -112,9 +125,33 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// offset in bytes of element (r, k) of a K-major tile; k counts 4-byte units
+// offset in bytes of element (r, k) of a K-major tile
+template <int MODE>
 __device__ __forceinline__ uint32_t tile_off(int r, int k) {
-    return (uint32_t)((r >> 3) * SBO + (k >> 2) * LBO + (r & 7) * 16 + (k & 3) * 4);
+    using C = Cfg<MODE>;
+    return (uint32_t)((r >> 3) * C::SBO + (k / C::CK) * C::LBO + (r & 7) * 16 + (k % C::CK) * (16 / C::CK));
+}
+
+// four consecutive K values of one row, converted and stored at tile offset o
+template <int MODE>
+__device__ __forceinline__ void put4(unsigned char *const (&t)[2], uint32_t o, float a, float b, float c, float d) {
+    if (MODE == CIR_PREC_TF32) {
+        *reinterpret_cast<uint4 *>(t[0] + o) = make_uint4(to_tf32(a), to_tf32(b), to_tf32(c), to_tf32(d));
+    } else {
+        const __nv_bfloat16 ha = __float2bfloat16_rn(a), hb = __float2bfloat16_rn(b);
+        const __nv_bfloat16 hc = __float2bfloat16_rn(c), hd = __float2bfloat16_rn(d);
+        const __nv_bfloat16 la = __float2bfloat16_rn(a - __bfloat162float(ha));
+        const __nv_bfloat16 lb = __float2bfloat16_rn(b - __bfloat162float(hb));
+        const __nv_bfloat16 lc = __float2bfloat16_rn(c - __bfloat162float(hc));
+        const __nv_bfloat16 ld = __float2bfloat16_rn(d - __bfloat162float(hd));
+        uint2 hi, lo;
+        hi.x = (uint32_t)__bfloat16_as_ushort(ha) | ((uint32_t)__bfloat16_as_ushort(hb) << 16);
+        hi.y = (uint32_t)__bfloat16_as_ushort(hc) | ((uint32_t)__bfloat16_as_ushort(hd) << 16);
+        lo.x = (uint32_t)__bfloat16_as_ushort(la) | ((uint32_t)__bfloat16_as_ushort(lb) << 16);
+        lo.y = (uint32_t)__bfloat16_as_ushort(lc) | ((uint32_t)__bfloat16_as_ushort(ld) << 16);
+        *reinterpret_cast<uint2 *>(t[0] + o) = hi;
+        *reinterpret_cast<uint2 *>(t[1] + o) = lo;
+    }
 }
 
 // One operand slice (rows r0..r0+127 of the MN dimension, k0..k0+TK-1) staged into
@@ -163,36 +200,38 @@ struct Slice {
             v[i] = x;
         }
     }
-    // write as TF32 into the K-major tile at byte address base
-    __device__ __forceinline__ void store_tf32(unsigned char *base) const {
+    // write into the K-major tile(s) of the mode (TF32, or BF16 hi and lo)
+    template <int MODE>
+    __device__ __forceinline__ void store(unsigned char *const (&base)[2]) const {
         const int t = threadIdx.x;
         #pragma unroll
         for (int i = 0; i < 8; i++) {
             if (KC) {
                 const int r = i * 16 + t / 8, k = 4 * (t % 8);
-                const uint4 u = make_uint4(to_tf32(v[i].x), to_tf32(v[i].y), to_tf32(v[i].z), to_tf32(v[i].w));
-                *reinterpret_cast<uint4 *>(base + tile_off(r, k)) = u;
+                put4<MODE>(base, tile_off<MODE>(r, k), v[i].x, v[i].y, v[i].z, v[i].w);
             } else if (i % 4 == 3) {
                 // v[i-3..i] are 4 k rows x 4 consecutive r: transpose to 4 r rows x 4 consecutive k
                 const int b = t + NTHREADS * (i / 4);
                 const int r = 4 * (b % 32), k = 4 * (b / 32);
                 const float4 a0 = v[i - 3], a1 = v[i - 2], a2 = v[i - 1], a3 = v[i];
-                *reinterpret_cast<uint4 *>(base + tile_off(r + 0, k)) = make_uint4(to_tf32(a0.x), to_tf32(a1.x), to_tf32(a2.x), to_tf32(a3.x));
-                *reinterpret_cast<uint4 *>(base + tile_off(r + 1, k)) = make_uint4(to_tf32(a0.y), to_tf32(a1.y), to_tf32(a2.y), to_tf32(a3.y));
-                *reinterpret_cast<uint4 *>(base + tile_off(r + 2, k)) = make_uint4(to_tf32(a0.z), to_tf32(a1.z), to_tf32(a2.z), to_tf32(a3.z));
-                *reinterpret_cast<uint4 *>(base + tile_off(r + 3, k)) = make_uint4(to_tf32(a0.w), to_tf32(a1.w), to_tf32(a2.w), to_tf32(a3.w));
+                put4<MODE>(base, tile_off<MODE>(r + 0, k), a0.x, a1.x, a2.x, a3.x);
+                put4<MODE>(base, tile_off<MODE>(r + 1, k), a0.y, a1.y, a2.y, a3.y);
+                put4<MODE>(base, tile_off<MODE>(r + 2, k), a0.z, a1.z, a2.z, a3.z);
+                put4<MODE>(base, tile_off<MODE>(r + 3, k), a0.w, a1.w, a2.w, a3.w);
             }
         }
     }
 };
 
-template <bool ACOL>
-__global__ void __launch_bounds__(NTHREADS) k_tc_gemm_tf32(GemmArgs g) {
+template <bool ACOL, int MODE>
+__global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
+    using C_ = Cfg<MODE>;
+    constexpr int TB = tile_bytes<MODE>();
+    constexpr int STAGE = 2 * C_::PARTS * TB;   // A and B parts of one stage
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sA[2] = {smem, smem + TILE_BYTES};
-    unsigned char *sB[2] = {smem + 2 * TILE_BYTES, smem + 3 * TILE_BYTES};
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 4 * TILE_BYTES);    // [2]
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + 4 * TILE_BYTES + 16);
+    // stage s: A parts at smem + s*STAGE, B parts after them
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * STAGE);    // [2]
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + 2 * STAGE + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int bz = blockIdx.z;
     const float *A = g.A + (size_t)bz * g.sA;
@@ -214,7 +253,7 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm_tf32(GemmArgs g) {
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    constexpr uint32_t IDESC = make_idesc(2);   // TF32
+    constexpr uint32_t IDESC = make_idesc(C_::FMT);
 
     Slice<!ACOL> la;    // A: K contiguous unless column-major
     Slice<false> lb;    // B: N contiguous
@@ -225,16 +264,27 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm_tf32(GemmArgs g) {
     for (int kt = 0; kt < KT; kt++) {
         const int s = kt & 1;
         if (kt >= 2) ok = mbar_wait(&bar[s], ((kt >> 1) - 1) & 1) && ok;   // MMAs that read stage s are done
-        la.store_tf32(sA[s]);
-        lb.store_tf32(sB[s]);
+        unsigned char *const pa[2] = {smem + s * STAGE, smem + s * STAGE + (C_::PARTS - 1) * TB};
+        unsigned char *const pb[2] = {smem + s * STAGE + C_::PARTS * TB, smem + s * STAGE + (2 * C_::PARTS - 1) * TB};
+        la.template store<MODE>(pa);
+        lb.template store<MODE>(pb);
         fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
             fence_after();
-            const uint32_t a0 = smem_addr(sA[s]), b0 = smem_addr(sB[s]);
             #pragma unroll
-            for (int ks = 0; ks < TK / 8; ks++)
-                mma_tf32(tmem, smem_desc(a0 + 2 * ks * LBO), smem_desc(b0 + 2 * ks * LBO), IDESC, (kt | ks) != 0);
+            for (int ks = 0; ks < TK / C_::KSTEP; ks++) {
+                const uint32_t o = 2 * ks * C_::LBO;   // two core matrices of K per instruction
+                const uint64_t ah = smem_desc<MODE>(smem_addr(pa[0]) + o), bh = smem_desc<MODE>(smem_addr(pb[0]) + o);
+                if (MODE == CIR_PREC_TF32) {
+                    mma_tf32(tmem, ah, bh, IDESC, (kt | ks) != 0);
+                } else {   // hi*hi + hi*lo + lo*hi
+                    const uint64_t al = smem_desc<MODE>(smem_addr(pa[1]) + o), bl = smem_desc<MODE>(smem_addr(pb[1]) + o);
+                    mma_f16(tmem, ah, bh, IDESC, (kt | ks) != 0);
+                    mma_f16(tmem, ah, bl, IDESC, 1u);
+                    mma_f16(tmem, al, bh, IDESC, 1u);
+                }
+            }
             mma_commit(&bar[s]);
         }
         if (kt + 1 < KT) {
@@ -289,24 +339,30 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm_tf32(GemmArgs g) {
     }
 }
 
+template <int MODE>
+__host__ __device__ constexpr size_t smem_bytes() { return 4 * (size_t)Cfg<MODE>::PARTS * tile_bytes<MODE>() + 64; }
+
+template <bool ACOL, int MODE>
+cudaError_t launch(const GemmArgs &g, int batch, cudaStream_t s) {
+    const size_t smem = smem_bytes<MODE>();
+    dim3 grid((g.N + TN - 1) / TN, (g.M + TM - 1) / TM, batch);
+    cudaError_t e = cudaFuncSetAttribute(k_tc_gemm<ACOL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_tc_gemm<ACOL, MODE><<<grid, NTHREADS, smem, s>>>(g);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
-size_t cir_tc_gemm_smem_bytes() { return 4 * (size_t)TILE_BYTES + 64; }
+size_t cir_tc_gemm_smem_bytes() { return smem_bytes<CIR_PREC_BF16X3>(); }
 
 cudaError_t cir_launch_tc_gemm(const GemmArgs &g, int batch, int precision, cudaStream_t s, int *launches) {
     if (g.epilogue == 1 && (g.N & 1)) return cudaErrorInvalidValue;
-    if (precision != CIR_PREC_TF32) return cudaErrorInvalidValue;
-    const size_t smem = cir_tc_gemm_smem_bytes();
-    dim3 grid((g.N + TN - 1) / TN, (g.M + TM - 1) / TM, batch);
     cudaError_t e;
-    if (g.a_colmajor) {
-        e = cudaFuncSetAttribute(k_tc_gemm_tf32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_tc_gemm_tf32<true><<<grid, NTHREADS, smem, s>>>(g);
-    } else {
-        e = cudaFuncSetAttribute(k_tc_gemm_tf32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_tc_gemm_tf32<false><<<grid, NTHREADS, smem, s>>>(g);
-    }
+    if (precision == CIR_PREC_TF32) e = g.a_colmajor ? launch<true, CIR_PREC_TF32>(g, batch, s) : launch<false, CIR_PREC_TF32>(g, batch, s);
+    else if (precision == CIR_PREC_BF16X3) e = g.a_colmajor ? launch<true, CIR_PREC_BF16X3>(g, batch, s) : launch<false, CIR_PREC_BF16X3>(g, batch, s);
+    else return cudaErrorInvalidValue;
     if (e != cudaSuccess) return e;
     if (launches) *launches += 1;
-    return cudaGetLastError();
+    return cudaSuccess;
 }

@@ -286,3 +286,40 @@ def test_propagate_tensor_core_tf32(lib, n):
         err = O.rel_l2(out[m], ref)
         assert err < 2e-3, err
         assert err > 1e-7, "tensor-core path produced FP32-exact output: is it running?"
+
+
+@pytest.mark.parametrize("n", [200, 1024])
+def test_propagate_tensor_core_bf16x3(lib, n):
+    """3-pass split-BF16 tcgen05 propagation: about 16 significant bits per operand."""
+    rng = np.random.default_rng(n + 11)
+    nprop, dt = 2, 0.010
+    A = np.stack([_sym(rng, n) for _ in range(nprop)])
+    F = (rng.standard_normal((nprop, n, n)) + 1j * rng.standard_normal((nprop, n, n))).astype(np.complex64)
+    with lib.Engine(lib.default_params(species="H2O", precision="bf16x3"), 8) as eng:
+        w, V = eng.eigh(A)
+        out = eng.propagate(V, w, np.float32(dt), F)
+    for m in range(nprop):
+        V64 = V[m].astype(np.float64)
+        ph = np.exp(1j * w[m].astype(np.float64) * np.float32(dt) / HBAR)
+        ref = (V64 * ph[None, :]) @ (V64.T @ F[m].astype(np.complex128))
+        err = O.rel_l2(out[m], ref)
+        assert 1e-8 < err < 5e-5, err
+
+
+MIXED_TOL = 1e-3   # relative L2 per spectrum for the mixed-precision forms
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("case", ["small_h2o", "multi_d2o_map1"])
+def test_run_mixed_precision_forms(lib, case, precision):
+    """The tensor-core forms against the FP64 oracle: every IR/Raman spectrum within
+    1e-3 relative L2 (the bound the mixed-precision form is held to)."""
+    meta, _ = load_golden(case)
+    prm, xyz, box, fos = _frames_for(lib, meta)
+    with lib.Engine(make_params(lib, prm, precision=precision), xyz.shape[1]) as eng:
+        out = eng.run(xyz, box, fos)
+    ref = O.run(prm, xyz, [box] * len(xyz), fos)
+    errs = {k: O.rel_l2(out[k], ref[k]) for k in ("tcf_ir", "tcf_vv", "tcf_vh", "ls_ir", "ls_vv", "ls_vh", "sw")}
+    print(case, precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, v in errs.items():
+        assert v < MIXED_TOL, (k, v)
