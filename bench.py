@@ -105,6 +105,19 @@ def gpu_identifier():
     return None
 
 
+def profiled_traffic():
+    """DRAM bytes per 1024 x 1024 matrix of the two eigensolver kernels, from the committed
+    ncu summary (profiles/k_eigh_n1024.md, line 'dram_bytes_per_matrix: tq=<B> qr=<B>')."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "k_eigh_n1024.md")):
+            if line.startswith("dram_bytes_per_matrix:"):
+                f = dict(x.split("=") for x in line.split(":", 1)[1].split())
+                return float(f["tq"]) + float(f["qr"])
+    except (OSError, KeyError, ValueError):
+        pass
+    return None
+
+
 def make_frames(cg, seed):
     p = cg.default_params(**JOB)
     fos = cg.frame_table(p, 0.010)
@@ -152,7 +165,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "tf32", "bf16x3"],
+                    help="arithmetic of the propagation GEMMs for the headline number")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP32 form beside it")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=8, help="frame-steps per CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -172,7 +187,6 @@ def main():
 
     # weak scaling: every rank runs its own 10-origin job on its own seeded trajectory
     p, xyz, box, fos = make_frames(cg, args.seed + rank)
-    p.precision = cg.PREC[args.precision] if hasattr(cg, "PREC") else 0
     steps_per_job = len(fos)
     stream = torch.cuda.current_stream()
     d_xyz = torch.from_numpy(xyz).cuda()
@@ -184,37 +198,49 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
-    with cg.Engine(p, xyz.shape[1]) as eng:
-        eng.set_stream(stream.cuda_stream)
-        for _ in range(max(args.warmup, 3)):
-            eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
-        eng.reset_stats()
-        torch.cuda.synchronize()
-        barrier()
-        clocks = ClockSampler(gpu_identifier())
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        t0.record(stream)
-        for _ in range(args.steps):
-            eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
-        t1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        clk = clocks.stop()
-        ms = t0.elapsed_time(t1)
-        st = eng.stats()
-        # end to end: pinned host positions in, all results out, inside the timed region
-        torch.cuda.synchronize()
-        barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            eng.run(h_xyz.data_ptr(), h_box.data_ptr(), fos, nframes=xyz.shape[0])
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        ms_e2e = e0.elapsed_time(e1)
+    def time_form(precision, steps, warmup, e2e=True, clocks=False):
+        """(device ms, e2e ms, stats, clock record) of `steps` jobs after `warmup` jobs."""
+        q = cg.default_params(**JOB, precision=precision)
+        res = {}
+        with cg.Engine(q, xyz.shape[1]) as eng:
+            eng.set_stream(stream.cuda_stream)
+            for _ in range(warmup):
+                eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+            eng.reset_stats()
+            torch.cuda.synchronize()
+            barrier()
+            sampler = ClockSampler(gpu_identifier()) if clocks else None
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(steps):
+                eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+            t1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            res["clk"] = sampler.stop() if sampler else None
+            res["ms"] = t0.elapsed_time(t1)
+            res["stats"] = eng.stats()
+            if e2e:
+                torch.cuda.synchronize()
+                barrier()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(steps):
+                    eng.run(h_xyz.data_ptr(), h_box.data_ptr(), fos, nframes=xyz.shape[0])
+                e1.record(stream)
+                torch.cuda.synchronize()
+                barrier()
+                res["ms_e2e"] = e0.elapsed_time(e1)
+        return res
+
+    warm = max(args.warmup, 3)
+    main_res = time_form(args.precision, args.steps, warm, e2e=True, clocks=True)
+    plain = None
+    if args.precision != "fp32" and not args.no_plain:
+        plain = time_form("fp32", args.steps, warm, e2e=False)
+    ms, ms_e2e, st, clk = main_res["ms"], main_res["ms_e2e"], main_res["stats"], main_res["clk"]
 
     if world > 1:
         t = torch.tensor([ms, ms_e2e], device="cuda")
@@ -229,26 +255,45 @@ def main():
     eig_ms_per_launch = st["ms_eig"] / args.steps          # one eigensolver launch per job (one chunk)
     eig_flops = 14.0 / 3.0 * n ** 3 * steps_per_job         # algorithmic flops per launch
     achieved = eig_flops / (eig_ms_per_launch * 1e-3) / 1e12
+    prop_flops = 8.0 * n ** 3 * JOB["nsamples"] * (JOB["ntcfpoints"] - 1)
+    prop_tflops = prop_flops / (st["ms_prop"] / args.steps * 1e-3) / 1e12
     nfft = JOB["ntcfpoints"] + JOB["nzeros"]
     nomega = 3001
     h2d = xyz.nbytes + xyz.shape[0] * 12 + fos.nbytes
     d2h = steps_per_job * 48 + nomega * 8 * 4 + 3 * nfft * 8
+    form = {"fp32": "plain FP32 (SIMT GEMMs)", "tf32": "mixed: TF32 tcgen05 propagation GEMMs",
+            "bf16x3": "mixed: 3-pass split-BF16 tcgen05 propagation GEMMs"}[args.precision]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": f"plain ({args.precision})", "nsamples": 10, "ntcfpoints": 250,
+        "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else f"f32+{args.precision}",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": form, "nsamples": 10, "ntcfpoints": 250,
                    "nchrom": n, "l2": "no flush needed: each step streams ~20 GB of Hamiltonians and eigenvectors "
                                      "(>> 129 MB L2)"},
         "stages_ms_per_step": {k: st[k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(st["kernel_launches"]),
-        "roofline": {"kernel": "k_eigh (batched eigensolver)", "bound": "tensor", "achieved": achieved,
+        "roofline": {"kernel": "k_eigh_tq + k_eigh_qr (batched eigensolver, one launch pair per job)",
+                     "bound": "tensor", "achieved": achieved,
                      "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
-                     "peak_kind": f"{pk_kind} bf16 dense (no FP32-SIMT peak is recorded)",
-                     "work": "14/3 N^3 flops per matrix x 2500 matrices per launch", "traffic": None},
+                     "peak_kind": f"{pk_kind} bf16 dense; the eigensolver runs on the FP32 SIMT pipes and is "
+                                  "latency/HBM bound, no FP32-SIMT peak is recorded",
+                     "work": "14/3 N^3 flops per matrix x 2500 matrices per launch",
+                     "traffic": (profiled_traffic() * steps_per_job) if profiled_traffic() else None,
+                     "traffic_note": "ncu dram__bytes_read+write per matrix (profiles/k_eigh_n1024.md) x 2500"},
+        "roofline_propagation": {"kernel": f"propagation GEMMs ({args.precision})", "bound": "tensor",
+                                 "achieved": prop_tflops, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                                 "frac": prop_tflops / pk["bf16_tflops"],
+                                 "work": "8 N^3 flops per origin-step (two real N x 2N x N GEMMs), 10 origins x "
+                                         "249 steps; time includes the correlation contraction"},
         "clocks": clk,
     }
+    if plain is not None:
+        line["plain_fp32"] = {"value": total_steps / (plain["ms"] * 1e-3) / world * world, "unit": UNIT,
+                              "ms_per_step": plain["ms"] / args.steps,
+                              "stages_ms_per_step": {k: plain["stats"][k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
+                              "mixed_over_plain": plain["ms"] / ms}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rates, cores = cpu_port_rate(args.seed, args.cpu_sample, 2)
         line["cpu_baseline"] = {"value": float(np.mean(rates)), "unit": UNIT, "cores": cores, "kind": "port",
