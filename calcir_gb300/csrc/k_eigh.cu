@@ -26,6 +26,7 @@
 // The leading dimension must be a multiple of 4 and A 16-byte aligned.
 #include "cir_device.cuh"
 #include <float.h>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -42,9 +43,32 @@ constexpr int EIG_KS = 16;     // QR sweeps per wavefront group in phase 3
 constexpr int EIG_W = EIG_KS + 1;
 constexpr int QR_PREFETCH = 4;  // Z columns loaded ahead of the wavefront in phase 3
 
-size_t tq_smem_bytes(int n) {
+// Blocked tridiagonalisation (orders above 256): panels of TB_NB columns, LAPACK sytrd/latrd
+// with lower storage.  Within a panel each column's matrix-vector product reads the lower
+// triangle of the trailing block as it stood at the start of the panel and corrects for the
+// panel's earlier columns with V and W; after the panel the trailing block is updated once,
+// A -= V W^T + W V^T, in TB_KC-column steps staged in shared memory.
+constexpr int TB_NB = 32;      // panel width
+constexpr int TB_KC = 8;       // panel columns per staged step of the trailing update
+constexpr int TB_ROWS = 128;   // rows of a trailing-update tile
+
+__host__ __device__ constexpr int tb_cols(int nt) { return 4 * (nt / 16); }   // its columns
+__host__ __device__ constexpr int tb_stage(int nt) { return TB_KC * (2 * TB_ROWS + 2 * tb_cols(nt)); }
+
+// floats of the shared work area: phase 2's reflector block, or phase 1's blocked state
+// (x, one partial product per warp, the staging tiles aliasing those, 4 panel vectors)
+__host__ __device__ inline size_t tq_union_floats(int n, int nt, bool blocked) {
+    const size_t n4 = (size_t)((n + 3) & ~3), n32 = (size_t)((n + 31) & ~31);
+    const size_t u = EIG_NB * n4;
+    if (!blocked) return u;
+    const size_t yw = n32 * (nt / 32), st = (size_t)tb_stage(nt);
+    const size_t need = n32 + (yw > st ? yw : st) + 4 * TB_NB;
+    return need > u ? need : u;
+}
+
+size_t tq_smem_bytes(int n, int nt, bool blocked) {
     const size_t n4 = (size_t)((n + 3) & ~3);
-    return sizeof(float) * (3 * n4 + EIG_NB * n4 + 64);
+    return sizeof(float) * (3 * n4 + tq_union_floats(n, nt, blocked) + 64);
 }
 
 size_t qr_smem_bytes(int n) {
@@ -221,7 +245,308 @@ __device__ __forceinline__ void apply_group(float *Z, int ld, const int (&row)[R
     }
 }
 
-template <int NT, int NMAX, int MINB>
+// ---- blocked tridiagonalisation (phase 1 for orders above 256) ----
+
+// y += A x on one 32 x 32 tile (I, J), I >= J, of the lower triangle, for both halves of
+// the symmetric matrix: A_IJ x_J into rows 32I.., A_IJ^T x_I into rows 32J...  Lane
+// (g, h) = (lane & 7, lane >> 3) loads rows 32I+4g..+3 of columns 32J+8h..+7 with 16-byte
+// accesses (each load instruction covers four whole 128-byte column segments).  The row
+// sums are reduced over h and the column sums over g by halving exchanges, after which lane
+// (g, h) owns row 32I+4g+h and column 32J+8h+g; both are added to this warp's own partial
+// product ywp, so no two lanes or warps write one word.  CHECK: diagonal tile (only r >= c
+// counted, the diagonal once) or a tile reaching past row n-1 (rows/columns >= n masked;
+// the padding rows below n may hold anything).
+template <bool CHECK>
+__device__ __forceinline__ void symv_tile(const float *__restrict__ A, int ld, int n, int I, int J,
+                                          const float *x, float *ywp, int lane) {
+    const int g = lane & 7, h = lane >> 3;
+    const int r0 = 32 * I + 4 * g, c0 = 32 * J + 8 * h;
+    float4 a[8];
+    #pragma unroll
+    for (int t = 0; t < 8; t++) {
+        if (!CHECK || (r0 < n && c0 + t < n)) a[t] = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(c0 + t) * ld + r0));
+        else a[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const float4 xr4 = *reinterpret_cast<const float4 *>(x + r0);
+    const float4 xc0 = *reinterpret_cast<const float4 *>(x + c0);
+    const float4 xc1 = *reinterpret_cast<const float4 *>(x + c0 + 4);
+    const float xr[4] = {xr4.x, xr4.y, xr4.z, xr4.w};
+    const float xc[8] = {xc0.x, xc0.y, xc0.z, xc0.w, xc1.x, xc1.y, xc1.z, xc1.w};
+    float yr[4] = {0.f, 0.f, 0.f, 0.f}, yc[8];
+    #pragma unroll
+    for (int t = 0; t < 8; t++) {
+        float av[4] = {a[t].x, a[t].y, a[t].z, a[t].w};
+        float s = 0.f;
+        #pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float ar = av[q], ac = av[q];
+            if (CHECK) {
+                const int r = r0 + q, c = c0 + t;
+                const bool ok = r < n && c < n;
+                ar = (ok && (I != J || r >= c)) ? ar : 0.f;
+                ac = (ok && (I != J || r > c)) ? ac : 0.f;
+            }
+            yr[q] = fmaf(ar, xc[t], yr[q]);
+            s = fmaf(ac, xr[q], s);
+        }
+        yc[t] = s;
+    }
+    // column sums over g (lane bits 0-2): keep the upper half where the bit is set
+    #pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const bool up = lane & 4;
+        const float send = up ? yc[i] : yc[i + 4], keep = up ? yc[i + 4] : yc[i];
+        yc[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    #pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const bool up = lane & 2;
+        const float send = up ? yc[i] : yc[i + 2], keep = up ? yc[i + 2] : yc[i];
+        yc[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+    {
+        const bool up = lane & 1;
+        const float send = up ? yc[0] : yc[1], keep = up ? yc[1] : yc[0];
+        yc[0] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+    }
+    // row sums over h (lane bits 3-4)
+    #pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const bool up = lane & 16;
+        const float send = up ? yr[i] : yr[i + 2], keep = up ? yr[i + 2] : yr[i];
+        yr[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    {
+        const bool up = lane & 8;
+        const float send = up ? yr[0] : yr[1], keep = up ? yr[1] : yr[0];
+        yr[0] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    ywp[r0 + h] += yr[0];
+    ywp[c0 + g] += yc[0];
+}
+
+// Trailing update after a panel: A[r][c] -= sum_j V[r][j] W[c][j] + W[r][j] V[c][j] for
+// q0 <= c <= r < n (lower triangle only), V = the panel's reflectors (columns p0.. of A,
+// with the unit element stored), W = the panel's W columns (Wb, leading dimension ld).
+// Tiles of TB_ROWS x BC on a grid starting at q0 rounded down to 4; thread (tr, tc) owns
+// rows 4tr..+3 and 64+4tr..+3 and columns 4tc..+3 of a tile.  V and W rows of the tile's
+// rows and columns are staged TB_KC panel columns at a time.
+template <int NT>
+__device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb, int n, int ld, int p0,
+                             int nb, float *stage) {
+    constexpr int BC = tb_cols(NT);
+    constexpr int F4 = (2 * TB_ROWS + 2 * BC) / 4;     // staged float4 per panel column
+    const int tid = threadIdx.x, tr = tid & 15, tc = tid >> 4;
+    const int q0 = p0 + nb;
+    const int R0 = q0 & ~3;
+    const int mr = n - R0;
+    const int ti = (mr + TB_ROWS - 1) / TB_ROWS, tj = (mr + BC - 1) / BC;
+    float *Vr = stage, *Wr = Vr + TB_KC * TB_ROWS, *Vc = Wr + TB_KC * TB_ROWS, *Wc = Vc + TB_KC * BC;
+    for (int I = 0; I < ti; I++) {
+        const int jmax = min(tj - 1, (TB_ROWS * I + TB_ROWS - 1) / BC);
+        for (int J = 0; J <= jmax; J++) {
+            const int rb = R0 + TB_ROWS * I, cb = R0 + BC * J;
+            const bool full = rb + TB_ROWS <= n && cb + BC <= n && cb >= q0 && cb + BC - 1 <= rb;
+            float a[8][4];
+            #pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = cb + 4 * tc + j;
+                #pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int r = rb + 64 * hh + 4 * tr;
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (full || (r < n && c < n)) v = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)c * ld + r));
+                    a[4 * hh + 0][j] = v.x; a[4 * hh + 1][j] = v.y; a[4 * hh + 2][j] = v.z; a[4 * hh + 3][j] = v.w;
+                }
+            }
+            for (int j0 = 0; j0 < nb; j0 += TB_KC) {
+                const int kc = min(TB_KC, nb - j0);
+                __syncthreads();   // the previous step's reads of the stage are done
+                for (int idx = tid; idx < kc * F4; idx += NT) {
+                    const int jj = idx / F4, o = idx - jj * F4;
+                    int row, part;
+                    if (o < TB_ROWS / 4) { part = 0; row = rb + 4 * o; }
+                    else if (o < TB_ROWS / 2) { part = 1; row = rb + 4 * (o - TB_ROWS / 4); }
+                    else if (o < TB_ROWS / 2 + BC / 4) { part = 2; row = cb + 4 * (o - TB_ROWS / 2); }
+                    else { part = 3; row = cb + 4 * (o - TB_ROWS / 2 - BC / 4); }
+                    const float *src = (part == 0 || part == 2) ? A + (size_t)(p0 + j0 + jj) * ld
+                                                                : Wb + (size_t)(j0 + jj) * ld;
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (row < n) v = *reinterpret_cast<const float4 *>(src + row);
+                    float *dst = part == 0 ? Vr + jj * TB_ROWS + (row - rb)
+                               : part == 1 ? Wr + jj * TB_ROWS + (row - rb)
+                               : part == 2 ? Vc + jj * BC + (row - cb)
+                                           : Wc + jj * BC + (row - cb);
+                    *reinterpret_cast<float4 *>(dst) = v;
+                }
+                __syncthreads();
+                for (int jj = 0; jj < kc; jj++) {
+                    const float4 v0 = *reinterpret_cast<const float4 *>(Vr + jj * TB_ROWS + 4 * tr);
+                    const float4 v1 = *reinterpret_cast<const float4 *>(Vr + jj * TB_ROWS + 64 + 4 * tr);
+                    const float4 w0 = *reinterpret_cast<const float4 *>(Wr + jj * TB_ROWS + 4 * tr);
+                    const float4 w1 = *reinterpret_cast<const float4 *>(Wr + jj * TB_ROWS + 64 + 4 * tr);
+                    const float4 vc4 = *reinterpret_cast<const float4 *>(Vc + jj * BC + 4 * tc);
+                    const float4 wc4 = *reinterpret_cast<const float4 *>(Wc + jj * BC + 4 * tc);
+                    const float vr[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+                    const float wr[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+                    const float vc[4] = {vc4.x, vc4.y, vc4.z, vc4.w};
+                    const float wc[4] = {wc4.x, wc4.y, wc4.z, wc4.w};
+                    #pragma unroll
+                    for (int i = 0; i < 8; i++)
+                        #pragma unroll
+                        for (int j = 0; j < 4; j++) a[i][j] = fmaf(-vr[i], wc[j], fmaf(-wr[i], vc[j], a[i][j]));
+                }
+            }
+            #pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = cb + 4 * tc + j;
+                #pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int r = rb + 64 * hh + 4 * tr;
+                    float *dst = A + (size_t)c * ld + r;
+                    if (full) {
+                        __stcg(reinterpret_cast<float4 *>(dst),
+                               make_float4(a[4 * hh][j], a[4 * hh + 1][j], a[4 * hh + 2][j], a[4 * hh + 3][j]));
+                    } else if (c < n && c >= q0) {
+                        #pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (r + q < n && r + q >= c) dst[q] = a[4 * hh + q][j];
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Phase 1 for orders above 256 (LAPACK ssytrd with lower storage, panels of TB_NB columns;
+// the same reflectors, d, e and tau conventions as the unblocked path).  Wb (TB_NB columns
+// of leading dimension ld) holds the panel's W; x, ywall (one partial product of order n32
+// per warp), pv (4 x TB_NB) and stage (aliasing ywall) are shared memory.
+template <int NT, int NMAX>
+__device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, int n, int ld, float *d, float *e,
+                                float *tau, float *x, float *ywall, float *pv, float *red) {
+    constexpr int NW = NT / 32;
+    constexpr int RW = (NMAX + NT - 1) / NT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n32 = (n + 31) & ~31;
+    const int tn = n32 >> 5;
+    float *sv = pv, *sw = pv + TB_NB, *t1 = pv + 2 * TB_NB, *t2 = pv + 3 * TB_NB;
+    float *ywp = ywall + (size_t)warp * n32;
+    for (int i = tid; i < n32; i += NT) x[i] = 0.f;
+    __syncthreads();
+    const int nref = n - 2;       // columns 0 .. n-3 carry reflectors
+    for (int p0 = 0; p0 < nref; p0 += TB_NB) {
+        const int nb = min(TB_NB, nref - p0);
+        for (int kk = 0; kk < nb; kk++) {
+            const int k = p0 + kk;
+            // (a) column k (rows k..n-1) with the panel's earlier updates applied
+            if (tid < kk) {
+                sv[tid] = A[(size_t)(p0 + tid) * ld + k];
+                sw[tid] = Wb[(size_t)tid * ld + k];
+            }
+            __syncthreads();
+            float part = 0.f;
+            for (int r = k + tid; r < n; r += NT) {
+                float v = A[(size_t)k * ld + r];
+                for (int jj = 0; jj < kk; jj++)
+                    v -= A[(size_t)(p0 + jj) * ld + r] * sw[jj] + Wb[(size_t)jj * ld + r] * sv[jj];
+                if (r == k) d[k] = v;
+                else if (r == k + 1) red[48] = v;
+                else { x[r] = v; part += v * v; }
+            }
+            const float xn2 = block_sum<NT>(part, red);
+            // (b) the reflector (slarfg convention: v[0] = 1, beta = -sign(alpha)*norm)
+            if (tid == 0) {
+                const float alpha = red[48];
+                float t = 0.f, beta = alpha, scale = 0.f;
+                if (xn2 > 0.f) {
+                    beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
+                    t = (beta - alpha) / beta;
+                    scale = 1.f / (alpha - beta);
+                }
+                tau[k] = t;
+                e[k] = beta;
+                red[49] = scale;
+            }
+            __syncthreads();
+            const float scale = red[49];
+            const float tk = tau[k];
+            // v (unit element at k+1, stored in A during the panel) into x; x[k] cleared
+            for (int r = k + tid; r < n; r += NT) {
+                const float v = r == k ? 0.f : (r == k + 1 ? 1.f : x[r] * scale);
+                x[r] = v;
+                if (r > k) A[(size_t)k * ld + r] = v;
+            }
+            const int j0 = (k + 1) >> 5;
+            for (int i = 32 * j0 + lane; i < n32; i += 32) ywp[i] = 0.f;
+            __syncthreads();
+            // (c) y = A22 v on the panel-start trailing block, plus t1 = W^T v, t2 = V^T v
+            {
+                const int tt = tn - j0;
+                const int ntiles = tt * (tt + 1) / 2;
+                int Ii = 0, Jj = warp;       // row-major enumeration of the lower triangle
+                while (Jj > Ii) { Jj -= Ii + 1; Ii++; }
+                for (int q = warp; q < ntiles; q += NW) {
+                    const int I = j0 + Ii, J = j0 + Jj;
+                    if (I == J || 32 * I + 32 > n) symv_tile<true>(A, ld, n, I, J, x, ywp, lane);
+                    else symv_tile<false>(A, ld, n, I, J, x, ywp, lane);
+                    Jj += NW;
+                    while (Jj > Ii) { Jj -= Ii + 1; Ii++; }
+                }
+            }
+            for (int dq = warp; dq < 2 * kk; dq += NW) {
+                const float *col = dq < kk ? Wb + (size_t)dq * ld : A + (size_t)(p0 + dq - kk) * ld;
+                float s = 0.f;
+                for (int r = k + 1 + lane; r < n; r += 32) s += col[r] * x[r];
+                s = warp_sum(s);
+                if (lane == 0) {
+                    if (dq < kk) t1[dq] = s;
+                    else t2[dq - kk] = s;
+                }
+            }
+            __syncthreads();
+            // (d) w = tau (y - V t1 - W t2), then w -= (tau/2)(w.v) v, into column kk of Wb
+            float wr[RW];
+            float dpart = 0.f;
+            #pragma unroll
+            for (int i = 0; i < RW; i++) {
+                const int r = k + 1 + tid + i * NT;
+                float w = 0.f;
+                if (r < n) {
+                    float y = 0.f;
+                    #pragma unroll
+                    for (int ww = 0; ww < NW; ww++) y += ywall[(size_t)ww * n32 + r];
+                    for (int jj = 0; jj < kk; jj++)
+                        y -= A[(size_t)(p0 + jj) * ld + r] * t1[jj] + Wb[(size_t)jj * ld + r] * t2[jj];
+                    w = tk * y;
+                    dpart += w * x[r];
+                }
+                wr[i] = w;
+            }
+            const float dot = block_sum<NT>(dpart, red);
+            const float half = -0.5f * tk * dot;
+            #pragma unroll
+            for (int i = 0; i < RW; i++) {
+                const int r = k + 1 + tid + i * NT;
+                if (r < n) Wb[(size_t)kk * ld + r] = wr[i] + half * x[r];
+            }
+            __syncthreads();
+        }
+        // (e) the trailing block beyond the panel
+        trail_update<NT>(A, Wb, n, ld, p0, nb, ywall);
+        __syncthreads();
+    }
+    if (tid == 0) {
+        d[n - 2] = A[(size_t)(n - 2) * ld + n - 2];
+        e[n - 2] = A[(size_t)(n - 2) * ld + n - 1];
+        d[n - 1] = A[(size_t)(n - 1) * ld + n - 1];
+        tau[n - 2] = 0.f;
+        e[n - 1] = 0.f;
+    }
+    __syncthreads();
+}
+
+template <int NT, int NMAX, int MINB, bool BLK>
 __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     constexpr int RMAX = (NMAX + 31) / 32;            // rows per lane, phase 2
     constexpr int QG = (NMAX + 4 * NT - 1) / (4 * NT); // 4-row groups per thread, phase 1
@@ -236,13 +561,18 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     float *d = smem;             // [n4]
     float *e = d + n4;           // [n4]
     float *tau = e + n4;         // [n4]
-    float *U = tau + n4;         // union region, EIG_NB*n4 floats (>= 4*n4)
-    float *red = U + (size_t)EIG_NB * n4;   // [64]
+    float *U = tau + n4;         // union region (tq_union_floats)
+    float *red = U + tq_union_floats(n, NT, BLK);   // [64]
 
     unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * 8 : nullptr;
     if (pt && tid == 0) pt[0] = globaltimer_ns();
     // ---------------- phase 1: tridiagonalisation ----------------
-    {
+    if constexpr (BLK) {
+        // W of the current panel lives in Z, which phase 2 overwrites
+        const int n32 = (n + 31) & ~31;
+        const int yws = max(n32 * NW, tb_stage(NT));
+        tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red);
+    } else {
         float *vp = U, *wp = U + n4, *vc = U + 2 * n4, *wc = U + 3 * n4;
         bool pending = false;
         for (int k = 0; k + 2 < n; k++) {
@@ -601,10 +931,10 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
 
 // MINB: resident blocks per SM the register budget is fitted to (3 while the spill stays
 // negligible; the order-2048 variant is fitted to 2 blocks).
-template <int NT, int NMAX, int MINB>
+template <int NT, int NMAX, int MINB, bool BLK>
 cudaError_t launch_tq(const EighArgs &a, int nmat, cudaStream_t s) {
-    auto kern = k_eigh_tq<NT, NMAX, MINB>;
-    const size_t smem = tq_smem_bytes(a.n);
+    auto kern = k_eigh_tq<NT, NMAX, MINB, BLK>;
+    const size_t smem = tq_smem_bytes(a.n, NT, BLK);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<nmat, NT, smem, s>>>(a);
@@ -636,10 +966,10 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.rot || !a.DE)
         return cudaErrorInvalidValue;
     cudaError_t e;
-    if (a.n <= 256) e = launch_tq<128, 256, 4>(a, nmat, s);
-    else if (a.n <= 512) e = launch_tq<256, 512, 3>(a, nmat, s);
-    else if (a.n <= 1024) e = launch_tq<256, 1024, 3>(a, nmat, s);
-    else e = launch_tq<256, 2048, 2>(a, nmat, s);
+    if (a.n <= 256) e = launch_tq<128, 256, 4, false>(a, nmat, s);
+    else if (a.n <= 512) e = launch_tq<256, 512, 3, true>(a, nmat, s);
+    else if (a.n <= 1024) e = launch_tq<256, 1024, 3, true>(a, nmat, s);
+    else e = launch_tq<256, 2048, 2, true>(a, nmat, s);
     if (e != cudaSuccess) return e;
     e = launch_qr(a, nmat, s);
     if (launches) *launches += 2;

@@ -69,7 +69,7 @@ def _check_eig(A, w, V, tol_scale=1.0):
     assert np.abs(A64 @ V64 - V64 * w[None, :]).max() <= 4e-6 * tol_scale * nrm * max(1.0, np.sqrt(n) / 4)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 64, 127, 128, 256, 432, 686, 1024, 2048])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 64, 127, 128, 256, 257, 301, 432, 513, 686, 1023, 1024, 2048])
 def test_eigh_random(lib, n):
     rng = np.random.default_rng(n)
     nmat = 3 if n <= 1024 else 1
@@ -80,11 +80,14 @@ def test_eigh_random(lib, n):
         _check_eig(A[m], w[m], V[m])
 
 
-def test_eigh_special_matrices(lib):
+@pytest.mark.parametrize("n", [96, 302])
+def test_eigh_special_matrices(lib, n):
+    """Zero, scaled identity, exact ties, a rank-one perturbation, diagonal, and a
+    tridiagonal with exact zeros (96: unblocked tridiagonalisation; 302: blocked, with a
+    padded leading dimension)."""
     rng = np.random.default_rng(5)
-    n = 96
     cases = [np.zeros((n, n), np.float32), np.eye(n, dtype=np.float32) * 3.0,
-             np.diag(np.repeat(np.arange(12, dtype=np.float32), 8)),          # exact ties
+             np.diag(np.repeat(np.arange(n // 8 + 1, dtype=np.float32), 8)[:n]),   # exact ties
              (np.eye(n) + np.outer(np.ones(n), np.ones(n)) / n).astype(np.float32),   # degenerate
              np.diag(rng.standard_normal(n).astype(np.float32)) * 500]
     t = np.zeros((n, n), np.float32)                                          # tridiagonal with zeros
