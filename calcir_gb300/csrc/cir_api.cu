@@ -89,23 +89,30 @@ static bool eigh_profiling() {
 }
 
 static void eigh_profile_report(const unsigned long long *dev, int nmat, cudaStream_t s) {
-    std::vector<unsigned long long> h((size_t)nmat * 8);
+    const int S = CIR_EIG_PROF_SLOTS;
+    std::vector<unsigned long long> h((size_t)nmat * S);
     if (cudaMemcpyAsync(h.data(), dev, h.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) return;
     cudaStreamSynchronize(s);
-    double sum[4] = {0, 0, 0, 0}, chase = 0, apply = 0, nrot = 0;
+    double tri = 0, fq = 0, qr = 0, srt = 0, chase = 0, apply = 0, nrot = 0, search = 0, sweeps = 0;
     unsigned long long t0 = ~0ull, t1 = 0;
     for (int m = 0; m < nmat; m++) {
-        for (int q = 0; q < 4; q++) sum[q] += (double)(h[m * 8 + q + 1] - h[m * 8 + q]);
-        t0 = std::min(t0, h[m * 8]);
-        t1 = std::max(t1, h[m * 8 + 4]);
-        chase += (double)h[m * 8 + 5];
-        apply += (double)h[m * 8 + 6];
-        nrot += (double)h[m * 8 + 7];
+        const unsigned long long *r = h.data() + (size_t)m * S;
+        tri += (double)(r[1] - r[0]);
+        fq += (double)(r[3] - r[2]);
+        qr += (double)(r[5] - r[4]);
+        srt += (double)(r[6] - r[5]);
+        t0 = std::min(t0, r[0]);
+        t1 = std::max(t1, r[6]);
+        chase += (double)r[7];
+        apply += (double)r[8];
+        nrot += (double)r[9];
+        search += (double)r[10];
+        sweeps += (double)r[11];
     }
     fprintf(stderr, "eigh profile: %d matrices, span %.3f ms; mean per block (ms): tridiag %.3f formQ %.3f qr %.3f "
-                    "(chase %.3f, apply %.3f, %.0f rotations) sort %.3f\n",
-            nmat, (t1 - t0) * 1e-6, sum[0] / nmat * 1e-6, sum[1] / nmat * 1e-6, sum[2] / nmat * 1e-6,
-            chase / nmat * 1e-6, apply / nmat * 1e-6, nrot / nmat, sum[3] / nmat * 1e-6);
+                    "(chase %.3f incl. block search %.3f, apply %.3f, %.0f rotations in %.0f sweeps) sort %.3f\n",
+            nmat, (t1 - t0) * 1e-6, tri / nmat * 1e-6, fq / nmat * 1e-6, qr / nmat * 1e-6, chase / nmat * 1e-6,
+            search / nmat * 1e-6, apply / nmat * 1e-6, nrot / nmat, sweeps / nmat, srt / nmat * 1e-6);
 }
 
 static int count_launch(cir_ctx *c, int k) {
@@ -310,8 +317,8 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     a.sweeps = c->buf[B_SWEEPS].as<unsigned long long>();
     a.nchrom_mol = c->p.nchrom_mol;
     if (eigh_profiling()) {
-        CK(c->buf[B_PROF].ensure((size_t)nmat * 8 * 8));
-        CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * 8 * 8, c->stream));
+        CK(c->buf[B_PROF].ensure((size_t)nmat * CIR_EIG_PROF_SLOTS * 8));
+        CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
         a.phase_ns = c->buf[B_PROF].as<unsigned long long>();
     }
     int launches = 0;
@@ -637,8 +644,8 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         e.avef = p.avef;
         e.omegaStart = p.omegaStart;
         if (eigh_profiling()) {
-            CK(c->buf[B_PROF].ensure((size_t)nbc * 8 * 8));
-            CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nbc * 8 * 8, c->stream));
+            CK(c->buf[B_PROF].ensure((size_t)nbc * CIR_EIG_PROF_SLOTS * 8));
+            CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nbc * CIR_EIG_PROF_SLOTS * 8, c->stream));
             e.phase_ns = c->buf[B_PROF].as<unsigned long long>();
         }
         CK(cir_launch_eigh(e, nbc, c->stream, &launches));

@@ -48,12 +48,14 @@ struct BuildArgs {
     CirMaps maps;
 };
 
+constexpr int CIR_EIG_PROF_SLOTS = 12;
+
 struct EighArgs {
     float *A;             // [nmat] matrices, column j of matrix m at A + m*mstride + j*ld
     float *W;             // [nmat][wstride] eigenvalues
     float *Z;             // scratch, same shape as A
     float2 *rot;          // scratch, cir_eigh_rot_bytes(n) per matrix
-    float *DE;            // scratch, cir_eigh_de_bytes(ld) per matrix (tridiagonal d, e)
+    float *DE;            // scratch, cir_eigh_de_bytes(ld) per matrix (tridiagonal d, e, tau)
     long long mstride;
     int wstride;
     int n, ld;
@@ -65,7 +67,10 @@ struct EighArgs {
     unsigned long long *out_of_range;
     int nomega, omegaStep, nchrom_mol;
     float avef, omegaStart;
-    unsigned long long *phase_ns;   // optional [nmat][5] %globaltimer at phase boundaries
+    // optional [nmat][CIR_EIG_PROF_SLOTS]: %globaltimer at the start and end of the
+    // tridiagonalisation, of forming Q, of the QR iteration and of the ordering (0-6), then the
+    // chase and apply times (ns), rotations, the chase's block-search time (ns) and sweeps
+    unsigned long long *phase_ns;
 };
 
 // kernel launchers (return cudaError_t of the launch)

@@ -1,16 +1,16 @@
 // Batched symmetric eigensolver for the exciton Hamiltonians (replaces magma_ssyevd_gpu,
-// calcIR.cu:420-448).  Two kernels, each with one thread block per matrix, so the SMs
-// work on independent frames at once: k_eigh_tq (phases 1-2, 256 threads) and k_eigh_qr
-// (phases 3-4, 128 threads: one chasing warp and three applying warps, four blocks per SM
-// so that four bulge chases overlap on every SM).
+// calcIR.cu:420-448).  Three kernels, each with one thread block per matrix, so the SMs
+// work on independent frames at once: k_eigh_tq (phase 1), k_eigh_formq (phase 2) and
+// k_eigh_qr (phases 3-4, 128 threads: one chasing warp and three applying warps, three
+// blocks per SM so that three bulge chases overlap on every SM).
 //
-//  1. Householder tridiagonalisation Q^T H Q = T (reflectors stored below the
-//     subdiagonal, as LAPACK sytd2).  The rank-2 update of step k-1 and the
-//     matrix-vector product of step k share one read/write pass over the trailing
-//     block; each thread streams four consecutive rows with 16-byte accesses.
-//  2. Q is formed explicitly in Z by backward accumulation of the reflectors, in blocks
-//     of EIG_NB reflectors staged in shared memory; each warp keeps one column segment of
-//     Z in registers while a block is applied.
+//  1. Householder tridiagonalisation Q^T H Q = T (reflectors stored below the subdiagonal,
+//     as LAPACK sytrd).  Orders above 256: blocked, lower storage, panels of TB_NB columns
+//     (tiled symmetric matrix-vector products, one rank-2*TB_NB update per panel).  Smaller
+//     orders: the rank-2 update of step k-1 and the matrix-vector product of step k share
+//     one read/write pass over the trailing block.
+//  2. Q is formed explicitly in Z by backward accumulation of the reflectors in compact WY
+//     blocks, each warp holding its rows of the block's reflectors in registers.
 //  3. Implicit symmetric QR on T with the Wilkinson shift (Golub & Van Loan, Alg. 8.3.2).
 //     Lane 0 of warp 0 chases the bulges of a group of EIG_KS sweeps (the bulge state is
 //     carried in registers) while the other warps apply the previous group to the rows
@@ -38,7 +38,6 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
-constexpr int EIG_NB = 8;      // reflectors per block in phase 2
 constexpr int EIG_KS = 16;     // QR sweeps per wavefront group in phase 3
 constexpr int EIG_W = EIG_KS + 1;
 constexpr int QR_PREFETCH = 4;  // Z columns loaded ahead of the wavefront in phase 3
@@ -55,15 +54,14 @@ constexpr int TB_ROWS = 128;   // rows of a trailing-update tile
 __host__ __device__ constexpr int tb_cols(int nt) { return 4 * (nt / 16); }   // its columns
 __host__ __device__ constexpr int tb_stage(int nt) { return TB_KC * (2 * TB_ROWS + 2 * tb_cols(nt)); }
 
-// floats of the shared work area: phase 2's reflector block, or phase 1's blocked state
-// (x, one partial product per warp, the staging tiles aliasing those, 4 panel vectors)
+// floats of phase 1's shared work area: the four vectors of the unblocked path, or the
+// blocked state (x, one partial product per warp, the staging tiles aliasing those, 4 panel
+// vectors)
 __host__ __device__ inline size_t tq_union_floats(int n, int nt, bool blocked) {
     const size_t n4 = (size_t)((n + 3) & ~3), n32 = (size_t)((n + 31) & ~31);
-    const size_t u = EIG_NB * n4;
-    if (!blocked) return u;
+    if (!blocked) return 4 * n4;
     const size_t yw = n32 * (nt / 32), st = (size_t)tb_stage(nt);
-    const size_t need = n32 + (yw > st ? yw : st) + 4 * TB_NB;
-    return need > u ? need : u;
+    return n32 + (yw > st ? yw : st) + 4 * TB_NB;
 }
 
 size_t tq_smem_bytes(int n, int nt, bool blocked) {
@@ -98,8 +96,12 @@ __device__ __forceinline__ bool negligible(float e, float d0, float d1, float ti
 
 struct Chaser {
     int cm, nsweep, status, cap;
+    int l;                         // start of the block of the previous sweep (-1: none yet)
+    int js;                        // largest split found during the previous sweep (-1: none)
     float tiny;
     long long nrot;
+    bool timed;                    // accumulate t_search (profiling only)
+    unsigned long long t_search;   // ns spent locating the unreduced block and the shift
 };
 
 // One implicit QR sweep with the Wilkinson shift on the trailing unreduced block of
@@ -108,45 +110,61 @@ struct Chaser {
 // rot points at slot s of a time-major group buffer: rotation i of this sweep is stored at
 // rot[(i + s) * EIG_KS], so the EIG_KS rotations applied at one wavefront step share one
 // 128-byte line.
+// The block [l, cm] is found without rescanning it: a sweep records the largest index whose
+// new off-diagonal is negligible, and a split, once used, is set to zero (as LAPACK ssteqr
+// does) so that it stays one when d[l] moves; only when the bottom deflates past every known
+// split is the block below scanned.
 __device__ bool qr_sweep(Chaser &ch, float *d, float *e, float2 *rot, int s_slot, int *lo, int *hi) {
+    const unsigned long long ts = ch.timed ? globaltimer_ns() : 0ull;
     int cm = ch.cm;
     while (cm > 0 && negligible(e[cm - 1], d[cm - 1], d[cm], ch.tiny)) { e[cm - 1] = 0.f; cm--; }
     ch.cm = cm;
     if (cm == 0) return false;
     if (ch.nsweep >= ch.cap) { ch.status = 1; return false; }
-    int l = cm - 1;
-    while (l > 0 && !negligible(e[l - 1], d[l - 1], d[l], ch.tiny)) l--;
+    int l;
+    if (ch.js >= 0 && cm > ch.js + 1) l = ch.js + 1;
+    else if (ch.js < 0 && ch.l >= 0 && cm > ch.l) l = ch.l;
+    else {
+        l = cm - 1;
+        while (l > 0 && !negligible(e[l - 1], d[l - 1], d[l], ch.tiny)) l--;
+    }
+    if (l > 0) e[l - 1] = 0.f;
+    ch.l = l;
     const float t = 0.5f * (d[cm - 1] - d[cm]);
     const float bb = e[cm - 1];
     const float den = t + copysignf(sqrtf(t * t + bb * bb), t);
     const float mu = d[cm] - (den != 0.f ? bb * bb / den : 0.f);
+    if (ch.timed) ch.t_search += globaltimer_ns() - ts;
     // bulge state in registers: dk = current d[k], ek = current e[k]; dk1/ek1 are the
     // untouched d[k+1], e[k+1], loaded one iteration ahead
     float x = d[l] - mu, z = e[l];
     float dk = d[l], ek = e[l];
     float dk1 = d[l + 1], ek1 = (l + 1 < cm) ? e[l + 1] : 0.f;
+    float dprev = 0.f;
+    int js = -1;
     for (int k = l; k < cm; k++) {
         const float dk2 = (k + 2 <= cm) ? d[k + 2] : 0.f;
         const float ek2 = (k + 2 < cm) ? e[k + 2] : 0.f;
         const float r2 = x * x + z * z;
-        float c = 1.f, s = 0.f, r = 0.f;
-        if (r2 >= 1e-30f) {
-            // reciprocal square root refined by one FMA-based Newton step (as accurate as a
-            // correctly rounded rsqrt for the orthogonality of the rotations)
-            const float i0 = rsqrtf(r2);
-            const float res = fmaf(-(r2 * i0), i0, 1.0f);
-            const float inv = fmaf(0.5f * i0, res, i0);
-            c = x * inv;
-            s = z * inv;
-            r = r2 * inv;
-        } else if (r2 > 0.f) {
+        // reciprocal square root refined by one FMA-based Newton step (as accurate as a
+        // correctly rounded rsqrt for the orthogonality of the rotations), computed without
+        // a branch; r2 below 1e-30 takes sqrt and division
+        const float i0 = rsqrtf(r2);
+        const float res = fmaf(-(r2 * i0), i0, 1.0f);
+        const float inv = fmaf(0.5f * i0, res, i0);
+        const bool big = r2 >= 1e-30f;
+        float c = big ? x * inv : 1.f, s = big ? z * inv : 0.f, r = big ? r2 * inv : 0.f;
+        if (!big && r2 > 0.f) {
             r = sqrtf(r2);
             c = x / r;
             s = z / r;
         }
         if (k > l) e[k - 1] = r;
         const float g = s * (dk - dk1) - 2.f * c * ek;
-        d[k] = dk - s * g;
+        const float dkn = dk - s * g;
+        d[k] = dkn;
+        if (k > l && negligible(r, dprev, dkn, ch.tiny)) js = k - 1;
+        dprev = dkn;
         const float dk1n = dk1 + s * g;
         const float ekn = c * s * (dk1 - dk) + (c * c - s * s) * ek;
         e[k] = ekn;
@@ -163,6 +181,8 @@ __device__ bool qr_sweep(Chaser &ch, float *d, float *e, float2 *rot, int s_slot
         ek1 = ek2;
     }
     d[cm] = dk;
+    if (negligible(e[cm - 1], dprev, dk, ch.tiny)) js = cm - 1;
+    ch.js = js;
     *lo = l;
     *hi = cm;
     ch.nsweep++;
@@ -548,7 +568,6 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
 
 template <int NT, int NMAX, int MINB, bool BLK>
 __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
-    constexpr int RMAX = (NMAX + 31) / 32;            // rows per lane, phase 2
     constexpr int QG = (NMAX + 4 * NT - 1) / (4 * NT); // 4-row groups per thread, phase 1
     constexpr int NW = NT / 32;
     extern __shared__ __align__(16) float smem[];
@@ -564,7 +583,7 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     float *U = tau + n4;         // union region (tq_union_floats)
     float *red = U + tq_union_floats(n, NT, BLK);   // [64]
 
-    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * 8 : nullptr;
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * CIR_EIG_PROF_SLOTS : nullptr;
     if (pt && tid == 0) pt[0] = globaltimer_ns();
     // ---------------- phase 1: tridiagonalisation ----------------
     if constexpr (BLK) {
@@ -719,65 +738,232 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
         __syncthreads();
     }
 
-    if (pt && tid == 0) pt[1] = globaltimer_ns();
-    // ---------------- phase 2: Q = H_0 H_1 ... H_{n-3} into Z ----------------
+    // d, e and tau for the next two kernels
+    float *de = a.DE + (size_t)blockIdx.x * 3 * ld;
+    for (int i = tid; i < n; i += NT) {
+        de[i] = d[i];
+        de[ld + i] = e[i];
+        de[2 * ld + i] = tau[i];
+    }
+    if (pt) {
+        __syncthreads();
+        if (tid == 0) pt[1] = globaltimer_ns();
+    }
+}
+
+// Sum NV per-lane values over the warp by halving exchanges (lane bit 4 first): lane L ends
+// with the warp sum of value xr_index<NV>(L), held by the 32/NV lanes that share it.
+template <int NV>
+__device__ __forceinline__ float xreduce(float (&y)[NV], int lane) {
+    constexpr int LG = NV == 32 ? 5 : NV == 16 ? 4 : NV == 8 ? 3 : NV == 4 ? 2 : NV == 2 ? 1 : 0;
+    #pragma unroll
+    for (int L = 0; L < LG; L++) {
+        const int o = 16 >> L, h = NV >> (L + 1);
+        const bool up = lane & o;
+        #pragma unroll
+        for (int i = 0; i < h; i++) {
+            const float send = up ? y[i] : y[i + h], keep = up ? y[i + h] : y[i];
+            y[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    #pragma unroll
+    for (int L = LG; L < 5; L++) y[0] += __shfl_xor_sync(0xffffffffu, y[0], 16 >> L);
+    return y[0];
+}
+
+template <int NV>
+__device__ __forceinline__ int xr_index(int lane) {
+    int idx = 0;
+    #pragma unroll
+    for (int L = 0; (NV >> (L + 1)) >= 1; L++)
+        if (lane & (16 >> L)) idx += NV >> (L + 1);
+    return idx;
+}
+
+// Phase 2: Q = H_0 H_1 ... H_{n-3} into Z by backward accumulation, NBQ reflectors at a
+// time in compact WY form (LAPACK slarft, forward, columnwise):
+// H_kb ... H_kb+NBQ-1 = I - V T V^T, applied as Z <- Z - V (T (V^T Z)) to the trailing
+// rows and columns.  Each warp owns interleaved 32-row chunks of the trailing rows and keeps
+// their NBQ reflector values in registers for the whole block, so a column costs NBQ FMAs
+// per element for V^T z and NBQ for the update with no shared-memory operand traffic; the
+// NBQ partial dots per column are summed over lanes by exchanges and over warps through
+// shared memory, CB columns at a time.  The next CB columns are copied into shared memory
+// (cp.async, each lane its own elements, so a per-thread wait suffices) while the current
+// ones are processed.  d, e, tau come from the tridiagonalisation kernel (DE rows 0-2).
+template <int NT, int NMAX, int NBQ, int CB>
+__host__ __device__ constexpr int fq_smem_floats() {
+    constexpr int NW = NT / 32, S = (NMAX + 32 * NW - 1) / (32 * NW);
+    return 2 * NW * CB * S * 32                                    // z double buffer
+           + NW * CB * NBQ + 2 * CB * NBQ + 2 * NBQ * NBQ + NBQ;
+}
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int sz = valid ? 4 : 0;   // 0: fill with zeros
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <int NT, int NMAX, int NBQ, int CB, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_eigh_formq(EighArgs a) {
+    constexpr int NW = NT / 32;
+    constexpr int S = (NMAX + 32 * NW - 1) / (32 * NW);   // row slots per lane
+    extern __shared__ __align__(16) float fsm[];
+    float *zb = fsm;                                 // [2][NW][CB][S][32]
+    float *part = zb + 2 * NW * CB * S * 32;         // [NW][CB][NBQ] per-warp partial V^T z
+    float *yfull = part + NW * CB * NBQ;             // [CB][NBQ] V^T z
+    float *uu = yfull + CB * NBQ;                    // [CB][NBQ] T V^T z
+    float *Gm = uu + CB * NBQ;                       // [NBQ][NBQ] V^T V (strict upper part)
+    float *Tm = Gm + NBQ * NBQ;                      // [NBQ][NBQ]
+    float *taus = Tm + NBQ * NBQ;                    // [NBQ]
+    const int n = a.n, ld = a.ld;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float *A = a.A + (size_t)blockIdx.x * a.mstride;
+    float *Z = a.Z + (size_t)blockIdx.x * a.mstride;
+    const float *tau_g = a.DE + (size_t)blockIdx.x * 3 * ld + 2 * ld;
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * CIR_EIG_PROF_SLOTS : nullptr;
+    if (pt && tid == 0) pt[2] = globaltimer_ns();
     for (size_t idx = tid; idx < (size_t)n * ld; idx += NT) {
         const int j = (int)(idx / ld), i = (int)(idx % ld);
         Z[idx] = (i == j) ? 1.f : 0.f;
     }
     __syncthreads();
-    {
-        const int nrefl = n - 2;
-        float *vb = U;   // [EIG_NB][n - r0]
-        for (int kb = nrefl > 0 ? ((nrefl - 1) / EIG_NB) * EIG_NB : -1; kb >= 0; kb -= EIG_NB) {
-            const int kend = min(kb + EIG_NB, nrefl);
-            const int r0 = kb + 1;
-            const int m = n - r0;
-            const int nb = kend - kb;
-            for (int idx = tid; idx < nb * m; idx += NT) {
-                const int kk = idx / m, i = r0 + idx % m, k = kb + kk;
-                vb[kk * m + (i - r0)] = i < k + 1 ? 0.f : (i == k + 1 ? 1.f : A[(size_t)k * ld + i]);
-            }
-            __syncthreads();
-            for (int j = r0 + warp; j < n; j += NW) {
-                float *col = Z + (size_t)j * ld + r0;
-                float q[RMAX];
+    const int nrefl = n - 2;
+    const int myidx = xr_index<NBQ>(lane);
+    const bool writer = (lane & ((32 / NBQ) - 1)) == 0;
+    float *zw = zb + (size_t)warp * CB * S * 32 + lane;   // this lane's slots: zw[buf*NW*CB*S*32 + (cc*S + t)*32]
+    for (int kb = nrefl > 0 ? ((nrefl - 1) / NBQ) * NBQ : -1; kb >= 0; kb -= NBQ) {
+        const int nb = min(NBQ, nrefl - kb);
+        const int r0 = kb + 1, m = n - r0;
+        // copy one batch of CB columns (this lane's rows) into buffer bf
+        auto fetch = [&](int c0, int bf) {
+            float *dst = zw + (size_t)bf * NW * CB * S * 32;
+            #pragma unroll
+            for (int cc = 0; cc < CB; cc++) {
+                const int j = c0 + cc;
                 #pragma unroll
-                for (int t = 0; t < RMAX; t++) {
-                    const int i = lane + 32 * t;
-                    q[t] = i < m ? col[i] : 0.f;
-                }
-                for (int kk = nb - 1; kk >= 0; kk--) {
-                    const float *v = vb + kk * m;
-                    float s = 0.f;
-                    #pragma unroll
-                    for (int t = 0; t < RMAX; t++) {
-                        const int i = lane + 32 * t;
-                        if (i < m) s += v[i] * q[t];
-                    }
-                    s = warp_sum(s) * tau[kb + kk];
-                    #pragma unroll
-                    for (int t = 0; t < RMAX; t++) {
-                        const int i = lane + 32 * t;
-                        if (i < m) q[t] -= s * v[i];
-                    }
-                }
-                #pragma unroll
-                for (int t = 0; t < RMAX; t++) {
-                    const int i = lane + 32 * t;
-                    if (i < m) col[i] = q[t];
+                for (int t = 0; t < S; t++) {
+                    const int rho = lane + 32 * (warp + NW * t);
+                    const bool ok = j < n && rho < m;
+                    cp_async4(dst + (cc * S + t) * 32, ok ? Z + (size_t)j * ld + r0 + rho : Z, ok);
                 }
             }
-            __syncthreads();
+            cp_async_commit();
+        };
+        fetch(r0, 0);
+        // this warp's rows of V: row r0 + rho, rho = lane + 32 (warp + NW t)
+        float vr[S][NBQ];
+        #pragma unroll
+        for (int t = 0; t < S; t++) {
+            const int rho = lane + 32 * (warp + NW * t);
+            const int r = r0 + rho;
+            #pragma unroll
+            for (int kk = 0; kk < NBQ; kk++) {
+                const int k = kb + kk;
+                float v = 0.f;
+                if (kk < nb && rho < m) v = r < k + 1 ? 0.f : (r == k + 1 ? 1.f : A[(size_t)k * ld + r]);
+                vr[t][kk] = v;
+            }
         }
+        // V^T V: G[l][j] = A[l'][j'+1] + sum_{r >= j'+2} A[l'][r] A[j'][r] (l < j, primes: +kb)
+        for (int pq = warp; pq < NBQ * (NBQ - 1) / 2; pq += NW) {
+            int l = 0, j = pq;
+            while (j >= NBQ - 1 - l) { j -= NBQ - 1 - l; l++; }
+            j += l + 1;
+            float g = 0.f;
+            if (j < nb) {
+                const float *cl = A + (size_t)(kb + l) * ld, *cj = A + (size_t)(kb + j) * ld;
+                for (int r = kb + j + 2 + lane; r < n; r += 32) g += cl[r] * cj[r];
+                g = warp_sum(g);
+                g += cl[kb + j + 1];
+            }
+            if (lane == 0) Gm[l * NBQ + j] = g;
+        }
+        if (tid < NBQ) taus[tid] = tid < nb ? tau_g[kb + tid] : 0.f;
+        __syncthreads();
+        if (warp == 0 && lane < NBQ) {
+            // row i = lane of T: T[i][i] = tau_i, T[i][j] = -tau_j sum_{l=i}^{j-1} T[i][l] G[l][j]
+            const int i = lane;
+            for (int j = 0; j < NBQ; j++) {
+                float t = 0.f;
+                if (j == i) t = taus[i];
+                else if (j > i) {
+                    float acc = 0.f;
+                    for (int l = i; l < j; l++) acc += Tm[i * NBQ + l] * Gm[l * NBQ + j];
+                    t = -taus[j] * acc;
+                }
+                Tm[i * NBQ + j] = t;
+            }
+        }
+        __syncthreads();
+        int bf = 0;
+        for (int c0 = r0; c0 < n; c0 += CB, bf ^= 1) {
+            if (c0 + CB < n) {
+                fetch(c0 + CB, bf ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            const float *zc = zw + (size_t)bf * NW * CB * S * 32;
+            // V^T z for CB columns: this warp's partial sums
+            #pragma unroll 1
+            for (int cc = 0; cc < CB; cc++) {
+                float y[NBQ];
+                #pragma unroll
+                for (int kk = 0; kk < NBQ; kk++) y[kk] = 0.f;
+                #pragma unroll
+                for (int t = 0; t < S; t++) {
+                    const float z = zc[(cc * S + t) * 32];
+                    #pragma unroll
+                    for (int kk = 0; kk < NBQ; kk++) y[kk] = fmaf(vr[t][kk], z, y[kk]);
+                }
+                const float ys = xreduce<NBQ>(y, lane);
+                if (writer) part[(warp * CB + cc) * NBQ + myidx] = ys;
+            }
+            __syncthreads();
+            for (int q = tid; q < CB * NBQ; q += NT) {
+                float sacc = 0.f;
+                #pragma unroll
+                for (int w = 0; w < NW; w++) sacc += part[w * CB * NBQ + q];
+                yfull[q] = sacc;
+            }
+            __syncthreads();
+            for (int q = tid; q < CB * NBQ; q += NT) {
+                const int cc = q / NBQ, i = q - cc * NBQ;
+                float sacc = 0.f;
+                for (int jj = i; jj < NBQ; jj++) sacc += Tm[i * NBQ + jj] * yfull[cc * NBQ + jj];
+                uu[q] = sacc;
+            }
+            __syncthreads();
+            // z -= V u
+            #pragma unroll 1
+            for (int cc = 0; cc < CB; cc++) {
+                const int j = c0 + cc;
+                if (j >= n) break;
+                float u[NBQ];
+                #pragma unroll
+                for (int kk = 0; kk < NBQ; kk++) u[kk] = uu[cc * NBQ + kk];
+                float *col = Z + (size_t)j * ld + r0;
+                #pragma unroll
+                for (int t = 0; t < S; t++) {
+                    const int rho = lane + 32 * (warp + NW * t);
+                    if (rho < m) {
+                        float zz = zc[(cc * S + t) * 32];
+                        #pragma unroll
+                        for (int kk = 0; kk < NBQ; kk++) zz = fmaf(-vr[t][kk], u[kk], zz);
+                        col[rho] = zz;
+                    }
+                }
+            }
+        }
+        __syncthreads();
     }
-
-    // d and e for the QR kernel
-    for (int i = tid; i < n; i += NT) {
-        a.DE[(size_t)blockIdx.x * 2 * ld + i] = d[i];
-        a.DE[(size_t)blockIdx.x * 2 * ld + ld + i] = e[i];
+    if (pt) {
+        __syncthreads();
+        if (tid == 0) pt[3] = globaltimer_ns();
     }
-    if (pt && tid == 0) pt[2] = globaltimer_ns();
 }
 
 template <int NT, int R>
@@ -794,10 +980,11 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
     float *e = d + n4;                               // [n4]
     float *U = e + n4;                               // [n4] ranks
     int *isc = reinterpret_cast<int *>(U + n4);      // [4*EIG_KS + 8]
-    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * 8 : nullptr;
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * CIR_EIG_PROF_SLOTS : nullptr;
+    if (pt && tid == 0) pt[4] = globaltimer_ns();
     for (int i = tid; i < n; i += NT) {
-        d[i] = a.DE[(size_t)blockIdx.x * 2 * ld + i];
-        e[i] = a.DE[(size_t)blockIdx.x * 2 * ld + ld + i];
+        d[i] = a.DE[(size_t)blockIdx.x * 3 * ld + i];
+        e[i] = a.DE[(size_t)blockIdx.x * 3 * ld + ld + i];
     }
     for (int q = tid; q < 2 * (n + EIG_KS) * EIG_KS; q += NT) rotg[q] = make_float2(1.f, 0.f);
     __syncthreads();
@@ -813,6 +1000,10 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
         ch.cap = 30 * n;
         ch.tiny = 0.f;
         ch.nrot = 0;
+        ch.timed = pt != nullptr;
+        ch.t_search = 0;
+        ch.l = -1;
+        ch.js = -1;
         unsigned long long t_chase = 0, t_apply = 0;
         if (tid == 0) {
             float tn = 0.f;
@@ -865,8 +1056,13 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
             __syncthreads();
             b ^= 1;
         }
-        if (pt && tid == 0) { pt[5] = t_chase; pt[7] = (unsigned long long)ch.nrot; }
-        if (pt && tid == 32) pt[6] = t_apply;
+        if (pt && tid == 0) {
+            pt[7] = t_chase;
+            pt[9] = (unsigned long long)ch.nrot;
+            pt[10] = ch.t_search;
+            pt[11] = (unsigned long long)ch.nsweep;
+        }
+        if (pt && tid == 32) pt[8] = t_apply;
         if (tid == 0) {
             if (a.status) a.status[blockIdx.x] = ch.status;
             if (a.sweeps) atomicAdd(a.sweeps, (unsigned long long)ch.nsweep);
@@ -874,7 +1070,7 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
         __syncthreads();
     }
 
-    if (pt && tid == 0) pt[3] = globaltimer_ns();
+    if (pt && tid == 0) pt[5] = globaltimer_ns();
     // ---------------- phase 4: ascending order, output, frequency distribution ----------------
     {
         int *rank = reinterpret_cast<int *>(U);
@@ -925,7 +1121,7 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
     }
     if (pt) {
         __syncthreads();
-        if (tid == 0) pt[4] = globaltimer_ns();
+        if (tid == 0) pt[6] = globaltimer_ns();
     }
 }
 
@@ -935,6 +1131,16 @@ template <int NT, int NMAX, int MINB, bool BLK>
 cudaError_t launch_tq(const EighArgs &a, int nmat, cudaStream_t s) {
     auto kern = k_eigh_tq<NT, NMAX, MINB, BLK>;
     const size_t smem = tq_smem_bytes(a.n, NT, BLK);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nmat, NT, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int NT, int NMAX, int NBQ, int CB, int MINB>
+cudaError_t launch_formq(const EighArgs &a, int nmat, cudaStream_t s) {
+    auto kern = k_eigh_formq<NT, NMAX, NBQ, CB, MINB>;
+    const size_t smem = sizeof(float) * fq_smem_floats<NT, NMAX, NBQ, CB>();
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<nmat, NT, smem, s>>>(a);
@@ -957,7 +1163,7 @@ cudaError_t launch_qr(const EighArgs &a, int nmat, cudaStream_t s) {
 
 size_t cir_eigh_rot_bytes(int n) { return sizeof(float2) * 2 * EIG_KS * (size_t)(n + EIG_KS); }
 
-size_t cir_eigh_de_bytes(int ld) { return sizeof(float) * 2 * (size_t)ld; }
+size_t cir_eigh_de_bytes(int ld) { return sizeof(float) * 3 * (size_t)ld; }
 
 int cir_eigh_max_n() { return 2048; }
 
@@ -971,8 +1177,12 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     else if (a.n <= 1024) e = launch_tq<256, 1024, 3, true>(a, nmat, s);
     else e = launch_tq<256, 2048, 2, true>(a, nmat, s);
     if (e != cudaSuccess) return e;
+    if (a.n <= 512) e = launch_formq<256, 512, 16, 8, 2>(a, nmat, s);
+    else if (a.n <= 1024) e = launch_formq<256, 1024, 16, 8, 2>(a, nmat, s);
+    else e = launch_formq<256, 2048, 8, 4, 2>(a, nmat, s);
+    if (e != cudaSuccess) return e;
     e = launch_qr(a, nmat, s);
-    if (launches) *launches += 2;
+    if (launches) *launches += 3;
     return e;
 }
 
@@ -1031,7 +1241,7 @@ extern "C" int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_
     const size_t mat = (size_t)n * ld * sizeof(float);
     const size_t need = align256(nmat * mat)                                   // Z
                         + align256(nmat * cir_eigh_rot_bytes(n))               // rotation groups
-                        + align256(nmat * cir_eigh_de_bytes(ld))               // d, e
+                        + align256(nmat * cir_eigh_de_bytes(ld))               // d, e, tau
                         + align256((size_t)nmat * sizeof(int))                 // status
                         + (pad ? align256(nmat * mat) : 0);                    // 16-byte aligned copy of A
     if (need > NOALLOC_SCRATCH_BYTES)
