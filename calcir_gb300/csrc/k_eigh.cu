@@ -40,7 +40,17 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 
 constexpr int EIG_KS = 16;     // QR sweeps per wavefront group in phase 3
 constexpr int EIG_W = EIG_KS + 1;
-constexpr int QR_PREFETCH = 4;  // Z columns loaded ahead of the wavefront in phase 3
+constexpr int QR_AHEAD = 12;    // Z columns copied ahead of the wavefront in phase 3
+
+// 4-byte asynchronous global-to-shared copy (src_size 0: zero fill), group commit and wait
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int sz = valid ? 4 : 0;   // 0: fill with zeros
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // Blocked tridiagonalisation (orders above 256): panels of TB_NB columns, LAPACK sytrd/latrd
 // with lower storage.  Within a panel each column's matrix-vector product reads the lower
@@ -69,9 +79,15 @@ size_t tq_smem_bytes(int n, int nt, bool blocked) {
     return sizeof(float) * (3 * n4 + tq_union_floats(n, nt, blocked) + 64);
 }
 
-size_t qr_smem_bytes(int n) {
+// d, e, ranks, the group bookkeeping, then the appliers' column ring (QR_AHEAD+1 slots of
+// rows x applying threads)
+__host__ __device__ inline size_t qr_ring_offset_floats(int n) {
     const size_t n4 = (size_t)((n + 3) & ~3);
-    return sizeof(float) * 3 * n4 + sizeof(int) * (4 * EIG_KS + 8);
+    return 3 * n4 + 4 * EIG_KS + 8;
+}
+
+size_t qr_smem_bytes(int n, int nt, int rows) {
+    return sizeof(float) * (qr_ring_offset_floats(n) + (size_t)(QR_AHEAD + 1) * rows * (nt - 32));
 }
 
 template <int NT>
@@ -197,21 +213,36 @@ __device__ bool qr_sweep(Chaser &ch, float *d, float *e, float2 *rot, int s_slot
 // applies its rotation i = tau - s.  Each row keeps the columns tau-EIG_KS+1 .. tau+1 in
 // registers w[0..EIG_KS] (slot j holds column tau-EIG_KS+1+j); rotation (s, tau-s) acts
 // on slots EIG_KS-1-s and EIG_KS-s and the window shifts by one slot per step, so every
-// column is read and written once per group.  Slots EIG_KS+1 .. EIG_KS+P hold columns
-// loaded P steps ahead.  row[j] < 0 marks an unused row slot.
-template <int R, int P>
+// column is read and written once per group.  Columns are streamed QR_AHEAD steps ahead
+// through a per-thread ring of QR_AHEAD+1 slots in shared memory (cp.async, so the DRAM
+// latency is covered without registers); ring + (slot * R + j) * stride is this thread's
+// element for row j.  row[j] < 0 marks an unused row slot.
+template <int R>
 __device__ __forceinline__ void apply_group(float *Z, int ld, const int (&row)[R], const float2 *rot,
-                                            int T0, int T1, int cmin, int cmax) {
-    constexpr int S = EIG_W + P;   // window slots
-    float w[R][S];
-    // columns T0-EIG_KS+1 .. T0+P into slots 0 .. EIG_KS-1+P
+                                            int T0, int T1, int cmin, int cmax, float *ring, int stride) {
+    constexpr int NS = QR_AHEAD + 1;
+    float w[R][EIG_W];
+    // columns T0-EIG_KS+1 .. T0 into slots 0 .. EIG_KS-1
     #pragma unroll
-    for (int v = 0; v < EIG_KS + P; v++) {
+    for (int v = 0; v < EIG_KS; v++) {
         const int c = T0 - EIG_KS + 1 + v;
         const bool ok = c >= cmin && c <= cmax;
         #pragma unroll
         for (int j = 0; j < R; j++) w[j][v] = (ok && row[j] >= 0) ? __ldcg(Z + (size_t)c * ld + row[j]) : 0.f;
     }
+    // columns T0+1 .. T0+QR_AHEAD into the ring (column c in slot c mod NS)
+    auto fetch = [&](int c) {
+        const int slot = c % NS;
+        const bool okc = c >= cmin && c <= cmax;
+        #pragma unroll
+        for (int j = 0; j < R; j++) {
+            const bool ok = okc && row[j] >= 0;
+            cp_async4(ring + (slot * R + j) * stride, ok ? Z + (size_t)c * ld + row[j] : Z, ok);
+        }
+        cp_async_commit();
+    };
+    #pragma unroll 1
+    for (int q = 1; q <= QR_AHEAD; q++) fetch(T0 + q);
     float4 nxt[EIG_KS / 2];
     #pragma unroll
     for (int q = 0; q < EIG_KS / 2; q++) nxt[q] = reinterpret_cast<const float4 *>(rot + (size_t)T0 * EIG_KS)[q];
@@ -223,11 +254,13 @@ __device__ __forceinline__ void apply_group(float *Z, int ld, const int (&row)[R
             #pragma unroll
             for (int q = 0; q < EIG_KS / 2; q++) nxt[q] = reinterpret_cast<const float4 *>(rot + (size_t)(tau + 1) * EIG_KS)[q];
         }
-        {   // column tau+1+P into the last slot
-            const int c = tau + 1 + P;
-            const bool ok = c >= cmin && c <= cmax;
+        {   // column tau+1 from the ring into the last slot; its slot's previous column (tau)
+            // was consumed a step ago, so column tau+1+QR_AHEAD may be fetched into ...(tau) mod NS
+            cp_async_wait<QR_AHEAD - 1>();
+            const int slot = (tau + 1) % NS;
             #pragma unroll
-            for (int j = 0; j < R; j++) w[j][S - 1] = (ok && row[j] >= 0) ? __ldcg(Z + (size_t)c * ld + row[j]) : 0.f;
+            for (int j = 0; j < R; j++) w[j][EIG_KS] = ring[(slot * R + j) * stride];
+            fetch(tau + 1 + QR_AHEAD);
         }
         #pragma unroll
         for (int s = 0; s < EIG_KS; s++) {
@@ -251,8 +284,9 @@ __device__ __forceinline__ void apply_group(float *Z, int ld, const int (&row)[R
         #pragma unroll
         for (int j = 0; j < R; j++)
             #pragma unroll
-            for (int v = 0; v < S - 1; v++) w[j][v] = w[j][v + 1];
+            for (int v = 0; v < EIG_KS; v++) w[j][v] = w[j][v + 1];
     }
+    cp_async_wait<0>();
     // after the last step the window holds columns T1-EIG_KS+2 .. T1+1 in slots 0..EIG_KS-1
     #pragma unroll
     for (int v = 0; v < EIG_KS; v++) {
@@ -797,14 +831,6 @@ __host__ __device__ constexpr int fq_smem_floats() {
            + NW * CB * NBQ + 2 * CB * NBQ + 2 * NBQ * NBQ + NBQ;
 }
 
-__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    const int sz = valid ? 4 : 0;   // 0: fill with zeros
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 template <int NT, int NMAX, int NBQ, int CB, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_eigh_formq(EighArgs a) {
@@ -1045,7 +1071,7 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
                     int row[R];
                     #pragma unroll
                     for (int j = 0; j < R; j++) row[j] = (r0 + j * napp + t < n) ? r0 + j * napp + t : -1;
-                    apply_group<R, QR_PREFETCH>(Z, ld, row, rb, T0, T1, cmin, cmax);
+                    apply_group<R>(Z, ld, row, rb, T0, T1, cmin, cmax, smem + qr_ring_offset_floats(n) + t, napp);
                 }
                 // back to identity for the group after next (the __syncthreads below orders
                 // this before the chase writes into the buffer again)
@@ -1152,7 +1178,7 @@ constexpr int QR_ROWS = 3;   // rows per applying thread; 3 blocks per SM withou
 
 cudaError_t launch_qr(const EighArgs &a, int nmat, cudaStream_t s) {
     auto kern = k_eigh_qr<QR_THREADS, QR_ROWS>;
-    const size_t smem = qr_smem_bytes(a.n);
+    const size_t smem = qr_smem_bytes(a.n, QR_THREADS, QR_ROWS);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<nmat, QR_THREADS, smem, s>>>(a);
