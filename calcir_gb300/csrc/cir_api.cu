@@ -49,7 +49,7 @@ enum {
     B_XYZ, B_BOX, B_FIDX, B_CXYZ, B_CBOX,          // run: frames and their gather
     B_A, B_W, B_M, B_F, B_G, B_M0,                 // run: matrices
     B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
-    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR,
+    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR, B_DC,
     B_COUNT
 };
 
@@ -289,12 +289,13 @@ extern "C" int cir_build_hamiltonian(cir_ctx *c, int nframes, const float *xyz, 
 extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     if (!c || !A || !w || nmat < 1 || n < 1) return cir_fail(CIR_ERR_ARG, "cir_eigh: bad argument");
     if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "cir_eigh: n = %d exceeds %d", n, cir_eigh_max_n());
+    if (nmat > 65535) return cir_fail(CIR_ERR_ARG, "cir_eigh: %d matrices in one call (at most 65535)", nmat);
     // the kernel wants a leading dimension that is a multiple of 4: stage through a padded copy
     const int ld = (n + 3) & ~3;
     const size_t mb = (size_t)n * ld * 4;
     CK(c->buf[B_PAD].ensure(nmat * mb));
     CK(c->buf[B_Z].ensure(nmat * mb));
-    CK(c->buf[B_ROT].ensure(nmat * cir_eigh_rot_bytes(n)));
+    CK(c->buf[B_DC].ensure(nmat * cir_dc_bytes(n, ld)));
     CK(c->buf[B_DE].ensure(nmat * cir_eigh_de_bytes(ld)));
     CK(c->buf[B_STATUS].ensure((size_t)nmat * 4));
     CK(c->buf[B_SWEEPS].ensure(8));
@@ -307,7 +308,7 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     a.A = c->buf[B_PAD].as<float>();
     a.W = c->buf[B_IN1].as<float>();
     a.Z = c->buf[B_Z].as<float>();
-    a.rot = c->buf[B_ROT].as<float2>();
+    a.DC = c->buf[B_DC].as<float>();
     a.DE = c->buf[B_DE].as<float>();
     a.mstride = (long long)n * ld;
     a.wstride = n;
@@ -547,13 +548,14 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
 
     // chunk: kn consecutive steps of all S origins per batch
-    const size_t per_step = (size_t)2 * n * ld * 4 + cir_eigh_rot_bytes(n) + cir_eigh_de_bytes(ld) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
-    size_t budget = (size_t)24 << 30;
+    const size_t per_step = (size_t)2 * n * ld * 4 + cir_dc_bytes(n, ld) + cir_eigh_de_bytes(ld) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
+    size_t budget = (size_t)64 << 30;
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
     int kn = (int)std::max<size_t>(1, budget / (per_step * S));
     if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / S);
     kn = std::min(kn, K);
+    kn = std::max(1, std::min(kn, 65535 / std::max(1, S)));   // matrices of a chunk index a grid dimension
 
     void *dxyz, *dbox;
     int rc;
@@ -568,7 +570,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     CK(c->buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
     CK(c->buf[B_A].ensure((size_t)nb * mstride * 4));
     CK(c->buf[B_Z].ensure((size_t)nb * mstride * 4));
-    CK(c->buf[B_ROT].ensure((size_t)nb * cir_eigh_rot_bytes(n)));
+    CK(c->buf[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
     CK(c->buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
     CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
     CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
@@ -626,7 +628,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         e.A = A;
         e.W = W;
         e.Z = c->buf[B_Z].as<float>();
-        e.rot = c->buf[B_ROT].as<float2>();
+        e.DC = c->buf[B_DC].as<float>();
         e.DE = c->buf[B_DE].as<float>();
         e.mstride = mstride;
         e.wstride = ld;

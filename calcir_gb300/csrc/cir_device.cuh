@@ -56,6 +56,8 @@ struct EighArgs {
     float *Z;             // scratch, same shape as A
     float2 *rot;          // scratch, cir_eigh_rot_bytes(n) per matrix
     float *DE;            // scratch, cir_eigh_de_bytes(ld) per matrix (tridiagonal d, e, tau)
+    float *DC;            // divide-and-conquer scratch, cir_dc_bytes(n, ld) per matrix, laid out
+                          // [3][nmat][mstride]; null selects the implicit-QR path (rot needed)
     long long mstride;
     int wstride;
     int n, ld;
@@ -78,6 +80,8 @@ cudaError_t cir_launch_build(const BuildArgs &a, int nframes, cudaStream_t s, in
 cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
 size_t cir_eigh_rot_bytes(int n);
 size_t cir_eigh_de_bytes(int ld);
+size_t cir_dc_bytes(int n, int ld);
+cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
 int cir_eigh_max_n();
 
 // batched SIMT FP32 GEMM, C = A * B (row-major B, C); A row- or column-major.

@@ -619,6 +619,7 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
 
     unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * CIR_EIG_PROF_SLOTS : nullptr;
     if (pt && tid == 0) pt[0] = globaltimer_ns();
+    if (a.status && tid == 0) a.status[blockIdx.x] = 0;
     // ---------------- phase 1: tridiagonalisation ----------------
     if constexpr (BLK) {
         // W of the current panel lives in Z, which phase 2 overwrites
@@ -1194,8 +1195,10 @@ size_t cir_eigh_de_bytes(int ld) { return sizeof(float) * 3 * (size_t)ld; }
 int cir_eigh_max_n() { return 2048; }
 
 cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches) {
-    if (a.n < 1 || a.n > cir_eigh_max_n() || nmat < 1 || (a.ld & 3) || a.ld < a.n) return cudaErrorInvalidValue;
-    if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.rot || !a.DE)
+    if (a.n < 1 || a.n > cir_eigh_max_n() || nmat < 1 || nmat > 65535 || (a.ld & 3) || a.ld < a.n)
+        return cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.DE ||
+        (!a.rot && !a.DC) || (a.DC && (reinterpret_cast<uintptr_t>(a.DC) & 15)))
         return cudaErrorInvalidValue;
     cudaError_t e;
     if (a.n <= 256) e = launch_tq<128, 256, 4, false>(a, nmat, s);
@@ -1207,8 +1210,10 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     else if (a.n <= 1024) e = launch_formq<256, 1024, 16, 8, 2>(a, nmat, s);
     else e = launch_formq<256, 2048, 8, 4, 2>(a, nmat, s);
     if (e != cudaSuccess) return e;
+    if (launches) *launches += 2;
+    if (a.DC) return cir_launch_dc(a, nmat, s, launches);
     e = launch_qr(a, nmat, s);
-    if (launches) *launches += 3;
+    if (launches) *launches += 1;
     return e;
 }
 
