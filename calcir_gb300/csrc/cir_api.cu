@@ -643,6 +643,10 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         e.nomega = nomega;
         e.omegaStep = p.omegaStep;
         e.nchrom_mol = p.nchrom_mol;
+        // eigenvectors need more than TF32's 10-bit mantissa: both mixed forms run the
+        // eigensolver's tensor-core products as 3-pass split BF16
+        e.precision = p.precision == CIR_PREC_FP32 ? CIR_PREC_FP32 : CIR_PREC_BF16X3;
+        e.err = c->buf[B_ERR].as<int>();
         e.avef = p.avef;
         e.omegaStart = p.omegaStart;
         if (eigh_profiling()) {

@@ -22,7 +22,8 @@
 //     row-major, and the eigenvalues ascending.
 //   * k_dc_gemm: Q_new = diag(Q1, Q2) U for every merge, as two products of the diagonal
 //     blocks with the matching rows of U (64 x 64 tiles, FP32).
-// The eigenvectors of H are then V = Q_H Q_T (Q_H formed by k_eigh_formq), one batched GEMM.
+// The eigenvectors of H are then V = Q_H Q_T (Q_H formed by k_eigh_formq), one batched GEMM:
+// FP32 in the plain form, the tensor-core GEMM (a.precision) in the mixed forms.
 #include "cir_device.cuh"
 #include <float.h>
 
@@ -521,12 +522,44 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
         if (e != cudaSuccess) return e;
         const int other = cur ^ 1;
         k_dc_merge<<<dim3(1 << level, nmat), DC_NT, smem, s>>>(a, level, KM, buf[cur], buf[other], buf[2]);
-        const int tiles = ((KM / 2 + 1 + 63) / 64) * ((KM + 63) / 64);
-        k_dc_gemm<<<dim3(tiles * (1 << level) * 2, nmat), 256, 0, s>>>(a, level, tiles, buf[cur], buf[2], buf[other]);
+        // the top two levels of the mixed forms on the tensor cores: one batched product per
+        // merge half when every offset keeps 16-byte alignment
+        bool tc = a.precision != CIR_PREC_FP32 && level <= 1;
+        for (int b = 0; tc && b < (1 << level); b++)
+            tc = (dc_off(level, b, n) & 3) == 0 && (dc_off(level + 1, 2 * b + 1, n) & 3) == 0;
+        if (tc) {
+            for (int b = 0; b < (1 << level); b++) {
+                const int a0 = dc_off(level, b, n), a1 = dc_off(level, b + 1, n), mid = dc_off(level + 1, 2 * b + 1, n);
+                for (int half = 0; half < 2; half++) {
+                    const int h0 = half ? mid : a0, hK = half ? a1 - mid : mid - a0;
+                    // column-major Q_new block = Q_half U_half; in the row-major view the
+                    // transpose: C^T = U_half^T Q_half^T
+                    GemmArgs g{};
+                    g.A = buf[2] + (size_t)h0 * ld + a0;        // U rows h0.., columns a0.. (row-major)
+                    g.B = buf[cur] + (size_t)h0 * ld + h0;      // Q block (column-major)
+                    g.C = buf[other] + (size_t)a0 * ld + h0;
+                    g.M = a1 - a0;
+                    g.N = hK;
+                    g.K = hK;
+                    g.lda = g.ldb = g.ldc = ld;
+                    g.sA = g.sB = g.sC = a.mstride;
+                    g.a_colmajor = true;
+                    g.epilogue = 0;
+                    g.err = a.err;
+                    e = cir_launch_tc_gemm(g, nmat, a.precision, s, nullptr);
+                    if (e != cudaSuccess) return e;
+                    nl++;
+                }
+            }
+            nl++;
+        } else {
+            const int tiles = ((KM / 2 + 1 + 63) / 64) * ((KM + 63) / 64);
+            k_dc_gemm<<<dim3(tiles * (1 << level) * 2, nmat), 256, 0, s>>>(a, level, tiles, buf[cur], buf[2], buf[other]);
+            nl += 2;
+        }
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         cur = other;
-        nl += 2;
     }
     // V = Q_H Q_T: in the row-major view of the column-major buffers, V^T = Q_T^T Q_H^T
     GemmArgs g{};
@@ -538,7 +571,9 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
     g.sA = g.sB = g.sC = a.mstride;
     g.a_colmajor = false;
     g.epilogue = 0;
-    e = cir_launch_gemm(g, nmat, s, nullptr);
+    g.err = a.err;
+    e = a.precision == CIR_PREC_FP32 ? cir_launch_gemm(g, nmat, s, nullptr)
+                                     : cir_launch_tc_gemm(g, nmat, a.precision, s, nullptr);
     if (e != cudaSuccess) return e;
     k_dc_finish<<<nmat, 256, 0, s>>>(a);
     nl += 2;
