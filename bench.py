@@ -106,16 +106,24 @@ def gpu_identifier():
 
 
 def profiled_traffic():
-    """DRAM bytes per 1024 x 1024 matrix of the two eigensolver kernels, from the committed
-    ncu summary (profiles/k_eigh_n1024.md, line 'dram_bytes_per_matrix: tq=<B> qr=<B>')."""
+    """DRAM bytes per 1024 x 1024 matrix of the tridiagonalisation kernel, from the committed
+    ncu summary (profiles/k_eigh_tq_n1024.md, line 'dram_bytes_per_matrix: <B>')."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", "k_eigh_n1024.md")):
+        for line in open(os.path.join(ROOT, "profiles", "k_eigh_tq_n1024.md")):
             if line.startswith("dram_bytes_per_matrix:"):
-                f = dict(x.split("=") for x in line.split(":", 1)[1].split())
-                return float(f["tq"]) + float(f["qr"])
-    except (OSError, KeyError, ValueError):
+                return float(line.split(":", 1)[1].split()[0])
+    except (OSError, ValueError, IndexError):
         pass
     return None
+
+
+def tridiag_bytes(n, nb=32):
+    """Algorithmic DRAM bytes of the blocked tridiagonalisation of one order-n matrix: each
+    column's matrix-vector product reads the lower triangle of its trailing block once, and
+    each panel of nb columns reads and writes the lower triangle beyond the panel once."""
+    sym = sum(4.0 * m * (m + 1) / 2 for m in range(1, n - 1))
+    upd = sum(8.0 * (n - q0) * (n - q0 + 1) / 2 for q0 in range(nb, n - 1, nb))
+    return sym + upd + 8.0 * 2 * 2   # + the final 2 x 2 block
 
 
 def make_frames(cg, seed):
@@ -252,9 +260,12 @@ def main():
 
     n = NMOL * 2
     pk, pk_kind = peaks()
-    eig_ms_per_launch = st["ms_eig"] / args.steps          # one eigensolver launch per job (one chunk)
-    eig_flops = 14.0 / 3.0 * n ** 3 * steps_per_job         # algorithmic flops per launch
-    achieved = eig_flops / (eig_ms_per_launch * 1e-3) / 1e12
+    eig_ms_per_launch = st["ms_eig"] / args.steps          # one eigensolver launch sequence per job (one chunk)
+    eig_flops = 14.0 / 3.0 * n ** 3 * steps_per_job         # nominal eigensolver flops per job
+    eig_tflops = eig_flops / (eig_ms_per_launch * 1e-3) / 1e12
+    tq_ms = st["ms_tridiag"] / args.steps                  # one tridiagonalisation launch per job
+    tq_bytes = tridiag_bytes(n) * steps_per_job
+    tq_gbs = tq_bytes / (tq_ms * 1e-3) / 1e9
     prop_flops = 8.0 * n ** 3 * JOB["nsamples"] * (JOB["ntcfpoints"] - 1)
     prop_tflops = prop_flops / (st["ms_prop"] / args.steps * 1e-3) / 1e12
     nfft = JOB["ntcfpoints"] + JOB["nzeros"]
@@ -274,14 +285,18 @@ def main():
         "stages_ms_per_step": {k: st[k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(st["kernel_launches"]),
-        "roofline": {"kernel": "k_eigh_tq + k_eigh_qr (batched eigensolver, one launch pair per job)",
-                     "bound": "tensor", "achieved": achieved,
-                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
-                     "peak_kind": f"{pk_kind} bf16 dense; the eigensolver runs on the FP32 SIMT pipes and is "
-                                  "latency/HBM bound, no FP32-SIMT peak is recorded",
-                     "work": "14/3 N^3 flops per matrix x 2500 matrices per launch",
+        "roofline": {"kernel": "k_eigh_tq (blocked lower-storage tridiagonalisation, one launch per job)",
+                     "bound": "hbm", "achieved": tq_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": tq_gbs / pk["hbm_gbs"], "peak_kind": f"{pk_kind} copy bandwidth (burst)",
+                     "work": "algorithmic bytes: per column the lower triangle of the trailing block, per "
+                             "32-column panel one read and write of the trailing lower triangle; "
+                             f"{tridiag_bytes(n) / 1e9:.3f} GB per 1024 x 1024 matrix x 2500 matrices per launch",
+                     "ms_per_launch": tq_ms,
                      "traffic": (profiled_traffic() * steps_per_job) if profiled_traffic() else None,
-                     "traffic_note": "ncu dram__bytes_read+write per matrix (profiles/k_eigh_n1024.md) x 2500"},
+                     "traffic_note": "ncu dram__bytes_read+write per matrix (profiles/k_eigh_tq_n1024.md) x 2500"},
+        "roofline_eigensolver": {"kernels": "tridiagonalisation, form Q, divide and conquer, V = Q_H Q_T",
+                                 "achieved": eig_tflops, "unit": "TFLOP/s",
+                                 "work": "14/3 N^3 nominal flops per matrix x 2500 matrices"},
         "roofline_propagation": {"kernel": f"propagation GEMMs ({args.precision})", "bound": "tensor",
                                  "achieved": prop_tflops, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                                  "frac": prop_tflops / pk["bf16_tflops"],

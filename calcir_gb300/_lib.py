@@ -60,6 +60,7 @@ class Stats(C.Structure):
     _fields_ = [
         ("kernel_launches", C.c_longlong), ("eig_sweeps", C.c_longlong), ("frame_steps", C.c_longlong),
         ("ms_build", C.c_double), ("ms_eig", C.c_double), ("ms_prop", C.c_double), ("ms_tcf", C.c_double),
+        ("ms_tridiag", C.c_double),
     ]
 
 

@@ -647,6 +647,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         // eigensolver's tensor-core products as 3-pass split BF16
         e.precision = p.precision == CIR_PREC_FP32 ? CIR_PREC_FP32 : CIR_PREC_BF16X3;
         e.err = c->buf[B_ERR].as<int>();
+        e.tq_done = ev[5];
         e.avef = p.avef;
         e.omegaStart = p.omegaStart;
         if (eigh_profiling()) {
@@ -700,6 +701,8 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         c->stats.ms_build += x;
         cudaEventElapsedTime(&x, ev[2], ev[3]);
         c->stats.ms_eig += x;
+        cudaEventElapsedTime(&x, ev[2], ev[5]);
+        c->stats.ms_tridiag += x;
         cudaEventElapsedTime(&x, ev[3], ev[4]);
         c->stats.ms_prop += x;
     }

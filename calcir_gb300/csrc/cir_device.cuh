@@ -56,6 +56,7 @@ struct EighArgs {
     float *Z;             // scratch, same shape as A
     float2 *rot;          // scratch, cir_eigh_rot_bytes(n) per matrix
     float *DE;            // scratch, cir_eigh_de_bytes(ld) per matrix (tridiagonal d, e, tau)
+    cudaEvent_t tq_done;  // recorded after the tridiagonalisation kernel when not null
     int precision;        // CIR_PREC_*: FP32, or the tensor-core form of the final V = Q_H Q_T product
     int *err;             // tensor-core kernels: set to 1 when a bounded wait gives up
     float *DC;            // divide-and-conquer scratch, cir_dc_bytes(n, ld) per matrix, laid out

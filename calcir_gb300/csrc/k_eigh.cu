@@ -1206,6 +1206,7 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     else if (a.n <= 1024) e = launch_tq<256, 1024, 3, true>(a, nmat, s);
     else e = launch_tq<256, 2048, 2, true>(a, nmat, s);
     if (e != cudaSuccess) return e;
+    if (a.tq_done && (e = cudaEventRecord(a.tq_done, s)) != cudaSuccess) return e;
     if (a.n <= 512) e = launch_formq<256, 512, 16, 8, 2>(a, nmat, s);
     else if (a.n <= 1024) e = launch_formq<256, 1024, 16, 8, 2>(a, nmat, s);
     else e = launch_formq<256, 2048, 8, 4, 2>(a, nmat, s);

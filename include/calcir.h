@@ -108,6 +108,7 @@ typedef struct cir_stats {
     long long eig_sweeps;               /* implicit QR sweeps, summed over matrices       */
     long long frame_steps;              /* frame-steps processed by cir_run*              */
     double    ms_build, ms_eig, ms_prop, ms_tcf;   /* device time per stage of cir_run*  */
+    double    ms_tridiag;               /* of ms_eig: the tridiagonalisation kernel       */
 } cir_stats;
 
 /* Parameters for the seeded synthetic water-box generator (replaces the .xtc source). */
