@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-from ._lib import (CIR_OK, EXE_PATH, LIB_PATH, PREC, CirError, Params, Result, Stats, Synth, check, load,
+from ._lib import (CIR_OK, EXE_PATH, LIB_PATH, PREC, CirError, Params, Result, Stats, Synth, TrajIn, check, load,
                    ptr)
 
 __all__ = ["Engine", "CirError", "default_params", "parse_input", "synth_trajectory", "write_traj",
@@ -115,6 +115,15 @@ def write_outputs(p: Params, res: dict) -> None:
         setattr(r, k, dp(res[k], np.float32))
     r.nls = len(res["ls_omega"])
     check(load().cir_write_outputs(C.byref(p), C.byref(r)))
+
+
+def _result_dict(bufs: dict, r) -> dict:
+    out = {k: (bufs[k][0::2] + 1j * bufs[k][1::2]) if k.startswith("tcf") else bufs[k] for k in bufs}
+    for k in ("ls_omega", "ls_ir", "ls_vv", "ls_vh"):
+        out[k] = out[k][:r.nls]
+    out["bins_out_of_range"] = r.bins_out_of_range
+    out["frame_steps_per_s"] = r.frame_steps_per_s
+    return out
 
 
 class Engine:
@@ -250,9 +259,35 @@ class Engine:
         for k, a in bufs.items():
             setattr(r, k, a.ctypes.data_as(C.POINTER(C.c_double if a.dtype == np.float64 else C.c_float)))
         check(self.lib.cir_run(self.h, nf, ptr(xyz), ptr(boxes), ptr(fos), C.byref(r)))
-        out = {k: (bufs[k][0::2] + 1j * bufs[k][1::2]) if k.startswith("tcf") else bufs[k] for k in bufs}
-        for k in ("ls_omega", "ls_ir", "ls_vv", "ls_vh"):
-            out[k] = out[k][:r.nls]
-        out["bins_out_of_range"] = r.bins_out_of_range
-        out["frame_steps_per_s"] = r.frame_steps_per_s
-        return out
+        return _result_dict(bufs, r)
+
+    def run_multi(self, trajectories) -> list[dict]:
+        """Many trajectories, boxes of uneven size allowed (cir_run_multi): ``trajectories``
+        is a list of (xyz (nframes, natoms, 3), boxes (nframes, 3) or (3,), frame_of_step or
+        None); xyz and boxes may be numpy arrays or contiguous float32 device tensors (boxes
+        then (nframes, 3)).  Returns one result dict per trajectory, as ``run`` would."""
+        keep, tin = [], (TrajIn * len(trajectories))()
+        for i, (xyz, boxes, fos) in enumerate(trajectories):
+            if hasattr(xyz, "data_ptr"):     # device tensors (contiguous float32), used in place
+                nf, na = int(xyz.shape[0]), int(xyz.shape[1])
+                px, pb = xyz.data_ptr(), boxes.data_ptr()
+            else:
+                xyz = np.ascontiguousarray(xyz, np.float32)
+                nf, na = xyz.shape[0], xyz.shape[1]
+                boxes = np.ascontiguousarray(np.broadcast_to(np.asarray(boxes, np.float32), (nf, 3)))
+                px, pb = xyz, boxes
+            fos = None if fos is None else np.ascontiguousarray(fos, np.int32)
+            keep += [xyz, boxes, fos]
+            tin[i].natoms, tin[i].nframes = na, nf
+            tin[i].xyz, tin[i].box, tin[i].frame_of_step = ptr(px), ptr(pb), ptr(fos)
+        ntcf, nom, nls = result_sizes(self.params)
+        allbufs, rs = [], (Result * len(trajectories))()
+        for i in range(len(trajectories)):
+            bufs = {k: np.zeros(2 * ntcf, np.float64) for k in ("tcf_ir", "tcf_vv", "tcf_vh")}
+            bufs.update({k: np.zeros(nom, np.float32) for k in ("omega", "sw", "pw", "rw", "rmw")})
+            bufs.update({k: np.zeros(nls, np.float32) for k in ("ls_omega", "ls_ir", "ls_vv", "ls_vh")})
+            for k, a in bufs.items():
+                setattr(rs[i], k, a.ctypes.data_as(C.POINTER(C.c_double if a.dtype == np.float64 else C.c_float)))
+            allbufs.append(bufs)
+        check(self.lib.cir_run_multi(self.h, len(trajectories), tin, rs))
+        return [_result_dict(allbufs[i], rs[i]) for i in range(len(trajectories))]

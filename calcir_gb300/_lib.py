@@ -42,6 +42,7 @@ class Params(C.Structure):
         ("synth_nmol", C.c_int), ("synth_seed", C.c_int), ("synth_frame_dt", C.c_float),
         ("synth_sigma_trans", C.c_float), ("synth_sigma_rot", C.c_float),
         ("precision", C.c_int), ("batch_frames", C.c_int), ("verbose", C.c_int),
+        ("cuda_graphs", C.c_int), ("autotune", C.c_int),
     ]
 
 
@@ -53,6 +54,13 @@ class Result(C.Structure):
         ("ls_omega", C.POINTER(C.c_float)), ("ls_ir", C.POINTER(C.c_float)), ("ls_vv", C.POINTER(C.c_float)),
         ("ls_vh", C.POINTER(C.c_float)), ("nls", C.c_int), ("bins_out_of_range", C.c_longlong),
         ("frame_steps_per_s", C.c_double),
+    ]
+
+
+class TrajIn(C.Structure):
+    _fields_ = [
+        ("natoms", C.c_int), ("nframes", C.c_int), ("xyz", C.c_void_p), ("box", C.c_void_p),
+        ("frame_of_step", C.c_void_p),
     ]
 
 
@@ -102,6 +110,7 @@ SIGNATURES = {
     "cir_spectral_density": [P, C.c_int, P, P, P, P],
     "cir_lineshape": [P, P, P, P, C.POINTER(C.c_int)],
     "cir_run": [P, C.c_int, P, P, P, C.POINTER(Result)],
+    "cir_run_multi": [P, C.c_int, C.POINTER(TrajIn), C.POINTER(Result)],
 }
 _RESTYPE = {"cir_version": C.c_char_p, "cir_last_error": C.c_char_p}
 

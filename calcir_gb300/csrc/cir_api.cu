@@ -19,6 +19,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <tuple>
 #include <vector>
 
 namespace {
@@ -49,11 +51,20 @@ enum {
     B_XYZ, B_BOX, B_FIDX, B_CXYZ, B_CBOX,          // run: frames and their gather
     B_A, B_W, B_M, B_F, B_G, B_M0,                 // run: matrices
     B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
-    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR, B_DC,
+    B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR, B_DC, B_TUNE,
     B_COUNT
 };
 
 }  // namespace
+
+// A captured step loop: its launch parameters (shapes, pointers, step range) and executable.
+struct GraphEntry {
+    std::vector<long long> key;
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+};
+
+using GemmShape = std::tuple<int, int, int, int, bool, int>;   // M, N, K, batch, A column-major, epilogue
 
 struct cir_ctx {
     cir_params p;
@@ -64,6 +75,8 @@ struct cir_ctx {
     cir_stats stats;
     cudaEvent_t ev[8];
     CirMaps maps;
+    std::map<GemmShape, int> gemm_tile;   // autotuner: SIMT tile shape per product shape
+    std::vector<GraphEntry> graphs;       // captured step loops, most recent last
 };
 
 #define CK(call)                                                                                        \
@@ -200,6 +213,8 @@ static int check_kernel_flag(cir_ctx *c) {
 extern "C" int cir_destroy(cir_ctx *c) {
     if (!c) return CIR_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
     for (auto &b : c->buf) b.release();
     for (auto &e : c->ev) cudaEventDestroy(e);
     if (c->own) cudaStreamDestroy(c->own);
@@ -231,15 +246,22 @@ extern "C" int cir_reset_stats(cir_ctx *c) {
     return CIR_OK;
 }
 
-static BuildArgs build_args(cir_ctx *c) {
+// One group of a run: ntraj trajectories of one system size, batched through every launch.
+struct Group {
+    int natoms, nmol, n, ld, ntraj;
+};
+
+static Group ctx_group(const cir_ctx *c) { return Group{c->natoms, c->nmol, c->n, c->ld, 1}; }
+
+static BuildArgs build_args(cir_ctx *c, const Group &g) {
     BuildArgs a;
     memset(&a, 0, sizeof a);
-    a.natoms = c->natoms;
+    a.natoms = g.natoms;
     a.natom_mol = c->p.natom_mol;
     a.nchrom_mol = c->p.nchrom_mol;
-    a.nmol = c->nmol;
-    a.n = c->n;
-    a.ld = c->ld;
+    a.nmol = g.nmol;
+    a.n = g.n;
+    a.ld = g.ld;
     a.imodel = c->p.imodel;
     a.ispecies = c->p.ispecies;
     a.avef = c->p.avef;
@@ -263,7 +285,7 @@ extern "C" int cir_build_hamiltonian(cir_ctx *c, int nframes, const float *xyz, 
     if (dip && (rc = stage_in(c, B_IN4, dip, (size_t)nframes * 3 * n * 4, &dD, false))) return rc;
     if (pol && (rc = stage_in(c, B_IN5, pol, (size_t)nframes * 6 * n * 4, &dP, false))) return rc;
     CK(c->buf[B_CT].ensure((size_t)nframes * CT_NROW * c->ld * 4));
-    BuildArgs a = build_args(c);
+    BuildArgs a = build_args(c, ctx_group(c));
     a.xyz = static_cast<const float *>(dx);
     a.box = static_cast<const float *>(db);
     a.ct = c->buf[B_CT].as<float>();
@@ -340,9 +362,59 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     return CIR_OK;
 }
 
+static GemmShape gemm_shape(const GemmArgs &g, int batch) {
+    return GemmShape(g.M, g.N, g.K, batch, g.a_colmajor, g.epilogue);
+}
+
+// The SIMT tile shape the autotuner chose for this product shape (128 x 128 if untuned).
+static int tuned_tile(cir_ctx *c, const GemmArgs &g, int batch) {
+    auto it = c->gemm_tile.find(gemm_shape(g, batch));
+    return it == c->gemm_tile.end() ? CIR_GEMM_TILE_128 : it->second;
+}
+
+// Autotuner: times both SIMT tile shapes of a product shape once per context (on scratch
+// operands of the same sizes, so the caller's data is untouched) and keeps the faster.
+// Must run outside stream capture.
+static int autotune_gemm(cir_ctx *c, const GemmArgs &g, int batch) {
+    if (!c->p.autotune || c->gemm_tile.count(gemm_shape(g, batch))) return CIR_OK;
+    const size_t a_el = (size_t)(g.a_colmajor ? g.K : g.M) * g.lda, b_el = (size_t)g.K * g.ldb,
+                 c_el = (size_t)g.M * g.ldc, w_el = g.epilogue == 1 ? (size_t)g.M : 0;
+    const size_t tot = (a_el + b_el + c_el + w_el + 16) * batch * sizeof(float);
+    CK(c->buf[B_TUNE].ensure(tot));
+    CK(cudaMemsetAsync(c->buf[B_TUNE].p, 0, tot, c->stream));
+    float *base = c->buf[B_TUNE].as<float>();
+    GemmArgs t = g;
+    t.A = base;
+    t.sA = (long long)a_el;
+    t.B = base + a_el * batch;
+    t.sB = (long long)b_el;
+    t.C = base + (a_el + b_el) * batch;
+    t.sC = (long long)c_el;
+    if (g.epilogue == 1) {
+        t.w = base + (a_el + b_el + c_el) * batch;
+        t.wstride = g.M;
+    }
+    float best = 1e30f;
+    int pick = CIR_GEMM_TILE_128;
+    for (int tile : {CIR_GEMM_TILE_128, CIR_GEMM_TILE_64}) {
+        CK(cir_launch_gemm(t, batch, c->stream, nullptr, tile));   // warm-up
+        CK(cudaEventRecord(c->ev[6], c->stream));
+        for (int r = 0; r < 3; r++) CK(cir_launch_gemm(t, batch, c->stream, nullptr, tile));
+        CK(cudaEventRecord(c->ev[7], c->stream));
+        CK(cudaEventSynchronize(c->ev[7]));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
+        if (ms < best) { best = ms; pick = tile; }
+    }
+    c->gemm_tile[gemm_shape(g, batch)] = pick;
+    if (c->p.verbose) printf("autotune: GEMM %d x %d x %d (batch %d): %s tiles\n", g.M, g.N, g.K, batch,
+                             pick == CIR_GEMM_TILE_64 ? "64 x 64" : "128 x 128");
+    return CIR_OK;
+}
+
 // F <- V diag(exp(+i w dt/hbar)) V^T F for `nprop` chains; all pointers on the device.
 static int propagate_dev(cir_ctx *c, int nprop, int n, const float *V, int ldv, long long sV, const float *w,
-                         int wstride, float dt, float *F, int ldf, long long sF, float *G) {
+                         int wstride, float dt, float *F, int ldf, long long sF, float *G, int &launches) {
     GemmArgs g1;
     memset(&g1, 0, sizeof g1);
     g1.A = V; g1.lda = ldv; g1.sA = sV; g1.a_colmajor = false;      // V^T as a row-major view of V
@@ -354,17 +426,15 @@ static int propagate_dev(cir_ctx *c, int nprop, int n, const float *V, int ldv, 
     GemmArgs g2 = g1;
     g2.A = V; g2.a_colmajor = true;                                   // V itself
     g2.B = G; g2.C = F; g2.epilogue = 0;
-    int launches = 0;
     if (c->p.precision == CIR_PREC_FP32) {
-        CK(cir_launch_gemm(g1, nprop, c->stream, &launches));
-        CK(cir_launch_gemm(g2, nprop, c->stream, &launches));
+        CK(cir_launch_gemm(g1, nprop, c->stream, &launches, tuned_tile(c, g1, nprop)));
+        CK(cir_launch_gemm(g2, nprop, c->stream, &launches, tuned_tile(c, g2, nprop)));
     } else {
         CK(c->buf[B_ERR].ensure(sizeof(int)));
         g1.err = g2.err = c->buf[B_ERR].as<int>();
         CK(cir_launch_tc_gemm(g1, nprop, c->p.precision, c->stream, &launches));
         CK(cir_launch_tc_gemm(g2, nprop, c->p.precision, c->stream, &launches));
     }
-    count_launch(c, launches);
     return CIR_OK;
 }
 
@@ -377,8 +447,10 @@ extern "C" int cir_propagate(cir_ctx *c, int nprop, int n, const float *V, const
     if ((rc = stage_in(c, B_IN1, w, (size_t)nprop * n * 4, &dW, true))) return rc;
     if ((rc = stage_in(c, B_IN2, F, nprop * mb * 2, &dF, true))) return rc;
     CK(c->buf[B_SCR].ensure(nprop * mb * 2));
+    int launches = 0;
     rc = propagate_dev(c, nprop, n, static_cast<float *>(dV), n, (long long)n * n, static_cast<float *>(dW), n, dt,
-                       static_cast<float *>(dF), 2 * n, 2LL * n * n, c->buf[B_SCR].as<float>());
+                       static_cast<float *>(dF), 2 * n, 2LL * n * n, c->buf[B_SCR].as<float>(), launches);
+    count_launch(c, launches);
     if (rc) return rc;
     if ((rc = stage_out(c, F, dF, nprop * mb * 2))) return rc;
     if (!is_device_ptr(F)) CK(cudaStreamSynchronize(c->stream));
@@ -524,48 +596,43 @@ __global__ void k_copy_m0(const float *m, long long sm_origin, int rows_ld, floa
 }
 }  // namespace
 
-extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *box, const int *frame_of_step,
-                       cir_result *r) {
-    if (!c || !xyz || !box || !r || nframes < 1) return cir_fail(CIR_ERR_ARG, "cir_run: bad argument");
-    const cir_params &p = c->p;
-    const int S = p.nsamples, K = p.ntcfpoints, n = c->n, ld = c->ld;
-    const int nomega = cir_nomega(&p);
-    const long long steps = (long long)S * K;
-    std::vector<int> fidx(steps);
-    if (frame_of_step) {
-        for (long long i = 0; i < steps; i++) {
-            if (frame_of_step[i] < 0 || frame_of_step[i] >= nframes)
-                return cir_fail(CIR_ERR_ARG, "frame_of_step[%lld] = %d outside [0, %d)", i, frame_of_step[i], nframes);
-            fidx[i] = frame_of_step[i];
-        }
-    } else {
-        if (nframes != steps) return cir_fail(CIR_ERR_ARG, "cir_run: %d frames for %lld frame-steps", nframes, steps);
-        for (long long i = 0; i < steps; i++) fidx[i] = (int)i;
-    }
-    const size_t nx = (size_t)nframes * c->natoms * 3;
-    const bool host_in = !is_device_ptr(xyz);
-    if (host_in && !all_finite(xyz, nx)) return cir_fail(CIR_ERR_NONFINITE, "positions contain NaN or Inf");
-    if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
+// Launch key of a captured step loop: every shape and pointer its launches depend on.
+static std::vector<long long> step_key(const Group &g, int St, int K, int k0, int kc, int precision, const void *A,
+                                       const void *W, const void *M, const void *F, const void *G, const void *M0,
+                                       const void *tcf, int tile1, int tile2) {
+    return {g.n, g.ld, St, K, k0, kc, precision, (long long)(uintptr_t)A, (long long)(uintptr_t)W,
+            (long long)(uintptr_t)M, (long long)(uintptr_t)F, (long long)(uintptr_t)G, (long long)(uintptr_t)M0,
+            (long long)(uintptr_t)tcf, tile1, tile2};
+}
 
-    // chunk: kn consecutive steps of all S origins per batch
-    const size_t per_step = (size_t)2 * n * ld * 4 + cir_dc_bytes(n, ld) + cir_eigh_de_bytes(ld) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
+// The frame-steps of one group: ntraj trajectories of one size, nsamples origins each.
+// dxyz / dbox hold all the group's frames on the device; fidx[(t*S + s)*K + k] is the frame
+// of step k of origin s of trajectory t.  res[t] receives trajectory t's results.
+static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float *dbox, const std::vector<int> &fidx,
+                     cir_result *res, double *ms_run) {
+    const cir_params &p = c->p;
+    const int S = p.nsamples, K = p.ntcfpoints, n = g.n, ld = g.ld, T = g.ntraj;
+    const int St = S * T;                                    // origins of the group
+    const int nomega = cir_nomega(&p);
+    const long long steps = (long long)St * K;
+
+    // chunk: kn consecutive steps of all St origins per batch
+    const size_t per_step = (size_t)2 * n * ld * 4 + cir_dc_bytes(n, ld) + cir_eigh_de_bytes(ld) +
+                            (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)g.natoms * 12 + 64;
     size_t budget = (size_t)64 << 30;
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
-    int kn = (int)std::max<size_t>(1, budget / (per_step * S));
-    if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / S);
+    int kn = (int)std::max<size_t>(1, budget / (per_step * St));
+    if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / St);
     kn = std::min(kn, K);
-    kn = std::max(1, std::min(kn, 65535 / std::max(1, S)));   // matrices of a chunk index a grid dimension
+    kn = std::max(1, std::min(kn, 65535 / std::max(1, St)));   // matrices of a chunk index a grid dimension
+    if (St > 65535) return cir_fail(CIR_ERR_ARG, "%d time origins in one group (at most 65535)", St);
 
-    void *dxyz, *dbox;
-    int rc;
-    if ((rc = stage_in(c, B_XYZ, xyz, nx * 4, &dxyz, true))) return rc;
-    if ((rc = stage_in(c, B_BOX, box, (size_t)nframes * 12, &dbox, true))) return rc;
     CK(c->buf[B_FIDX].ensure((size_t)steps * 4));
     CK(cudaMemcpyAsync(c->buf[B_FIDX].p, fidx.data(), (size_t)steps * 4, cudaMemcpyHostToDevice, c->stream));
-    const int nb = S * kn;
+    const int nb = St * kn;
     const long long mstride = (long long)n * ld;
-    CK(c->buf[B_CXYZ].ensure((size_t)nb * c->natoms * 12));
+    CK(c->buf[B_CXYZ].ensure((size_t)nb * g.natoms * 12));
     CK(c->buf[B_CBOX].ensure((size_t)nb * 12));
     CK(c->buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
     CK(c->buf[B_A].ensure((size_t)nb * mstride * 4));
@@ -575,24 +642,24 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
     CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
     CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
-    CK(c->buf[B_F].ensure((size_t)S * n * 2 * ld * 4));
-    CK(c->buf[B_G].ensure((size_t)S * n * 2 * ld * 4));
-    CK(c->buf[B_M0].ensure((size_t)S * 9 * ld * 4));
+    CK(c->buf[B_F].ensure((size_t)St * n * 2 * ld * 4));
+    CK(c->buf[B_G].ensure((size_t)St * n * 2 * ld * 4));
+    CK(c->buf[B_M0].ensure((size_t)St * 9 * ld * 4));
     CK(c->buf[B_TCF].ensure((size_t)steps * 6 * 8));
-    CK(c->buf[B_HCNT].ensure((size_t)nomega * 8));
-    CK(c->buf[B_HIPR].ensure((size_t)nomega * 8));
-    CK(c->buf[B_HMIPR].ensure((size_t)nomega * 8));
-    CK(c->buf[B_OOR].ensure(8));
+    CK(c->buf[B_HCNT].ensure((size_t)T * nomega * 8));
+    CK(c->buf[B_HIPR].ensure((size_t)T * nomega * 8));
+    CK(c->buf[B_HMIPR].ensure((size_t)T * nomega * 8));
+    CK(c->buf[B_OOR].ensure((size_t)T * 8));
     CK(c->buf[B_SWEEPS].ensure(8));
-    CK(c->buf[B_SW].ensure((size_t)nomega * 8));
+    CK(c->buf[B_SW].ensure((size_t)T * nomega * 8));
     CK(c->buf[B_MU2].ensure((size_t)ld * 4));
     CK(cudaMemsetAsync(c->buf[B_TCF].p, 0, (size_t)steps * 48, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_HCNT].p, 0, (size_t)nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_HIPR].p, 0, (size_t)nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_HMIPR].p, 0, (size_t)nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_OOR].p, 0, 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_HCNT].p, 0, (size_t)T * nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_HIPR].p, 0, (size_t)T * nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_HMIPR].p, 0, (size_t)T * nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_OOR].p, 0, (size_t)T * 8, c->stream));
     CK(cudaMemsetAsync(c->buf[B_SWEEPS].p, 0, 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_SW].p, 0, (size_t)nomega * 8, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_SW].p, 0, (size_t)T * nomega * 8, c->stream));
     CK(cudaMemsetAsync(c->buf[B_STATUS].p, 0, (size_t)nb * 4, c->stream));
 
     float *A = c->buf[B_A].as<float>(), *W = c->buf[B_W].as<float>(), *M = c->buf[B_M].as<float>();
@@ -600,17 +667,28 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     double *tcf = c->buf[B_TCF].as<double>();
     int launches = 0;
     cudaEvent_t *ev = c->ev;
+    int rc;
+
+    // the propagation products of this group, tuned before anything is timed or captured
+    GemmArgs g1{}, g2{};
+    g1.M = n; g1.N = 2 * n; g1.K = n; g1.lda = ld; g1.ldb = g1.ldc = 2 * ld; g1.a_colmajor = false; g1.epilogue = 1;
+    g2 = g1; g2.a_colmajor = true; g2.epilogue = 0;
+    if (p.precision == CIR_PREC_FP32) {
+        if ((rc = autotune_gemm(c, g1, St))) return rc;
+        if ((rc = autotune_gemm(c, g2, St))) return rc;
+    }
+    const int tile1 = tuned_tile(c, g1, St), tile2 = tuned_tile(c, g2, St);
+
     CK(cudaEventRecord(ev[0], c->stream));
     for (int k0 = 0; k0 < K; k0 += kn) {
         const int kc = std::min(kn, K - k0);
-        const int nbc = S * kc;
+        const int nbc = St * kc;
         CK(cudaEventRecord(ev[1], c->stream));
-        k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(static_cast<float *>(dxyz), static_cast<float *>(dbox),
-                                                             c->buf[B_FIDX].as<int>(), c->natoms, S, kc, K, k0,
-                                                             c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
+        k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(dxyz, dbox, c->buf[B_FIDX].as<int>(), g.natoms, St, kc, K,
+                                                             k0, c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
         CK(cudaGetLastError());
         launches++;
-        BuildArgs a = build_args(c);
+        BuildArgs a = build_args(c, g);
         a.xyz = c->buf[B_CXYZ].as<float>();
         a.box = c->buf[B_CBOX].as<float>();
         a.ct = c->buf[B_CT].as<float>();
@@ -640,6 +718,7 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         e.hist_ipr = c->buf[B_HIPR].as<double>();
         e.hist_mipr = c->buf[B_HMIPR].as<double>();
         e.out_of_range = c->buf[B_OOR].as<unsigned long long>();
+        e.hist_group = S * kc;        // the chunk's matrices of one trajectory share its histograms
         e.nomega = nomega;
         e.omegaStep = p.omegaStep;
         e.nchrom_mol = p.nchrom_mol;
@@ -659,40 +738,81 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         if (e.phase_ns) eigh_profile_report(e.phase_ns, nbc, c->stream);
         CK(cudaEventRecord(ev[3], c->stream));
         if (k0 == 0) {
-            // spectral density at step 0 of every origin (calcIR.cu:456-482)
-            for (int s = 0; s < S; s++) {
+            // spectral density at step 0 of every origin (calcIR.cu:456-482), per trajectory
+            for (int s = 0; s < St; s++) {
                 const size_t b = (size_t)s * kc;
                 CK(cir_launch_spectral(A + b * mstride, ld, W + b * ld, M + b * 9 * ld, ld, n, c->buf[B_MU2].as<float>(),
-                                       c->buf[B_SW].as<double>(), nomega, p.omegaStart, p.omegaStep, p.t1, p.avef,
-                                       c->stream, &launches));
+                                       c->buf[B_SW].as<double>() + (size_t)(s / S) * nomega, nomega, p.omegaStart,
+                                       p.omegaStep, p.t1, p.avef, c->stream, &launches));
             }
             // F = I and the t = 0 vectors (calcIR.cu:577-594)
-            CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, S, c->stream, &launches));
-            k_copy_m0<<<dim3(4, S), 256, 0, c->stream>>>(M, (long long)kc * 9 * ld, ld, M0);
+            CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, St, c->stream, &launches));
+            k_copy_m0<<<dim3(4, St), 256, 0, c->stream>>>(M, (long long)kc * 9 * ld, ld, M0);
             CK(cudaGetLastError());
             launches++;
         }
-        for (int k = k0; k < k0 + kc; k++) {
-            const int kk = k - k0;
-            if (k > 0) {   // F <- V_k exp(i L_k dt/hbar) V_k^T F for every origin (calcIR.cu:596-617)
-                int rc2 = propagate_dev(c, S, n, A + (size_t)kk * mstride, ld, (long long)kc * mstride, W + (size_t)kk * ld,
-                                        kc * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G);
-                if (rc2) return rc2;
+        // the chunk's steps: F <- V_k exp(i L_k dt/hbar) V_k^T F for every origin
+        // (calcIR.cu:596-617), then the correlation terms (calcIR.cu:628-745)
+        auto run_steps = [&](int &nl) -> int {
+            for (int k = k0; k < k0 + kc; k++) {
+                const int kk = k - k0;
+                if (k > 0) {
+                    int rc2 = propagate_dev(c, St, n, A + (size_t)kk * mstride, ld, (long long)kc * mstride,
+                                            W + (size_t)kk * ld, kc * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);
+                    if (rc2) return rc2;
+                }
+                TcfArgs t;
+                memset(&t, 0, sizeof t);
+                t.F = F;
+                t.sF = (long long)n * 2 * ld;
+                t.m0 = M0;
+                t.sm0 = 9LL * ld;
+                t.mt = M + (size_t)kk * 9 * ld;
+                t.smt = (long long)kc * 9 * ld;
+                t.out = tcf + (size_t)k * 6;
+                t.sout = (long long)K * 6;
+                t.n = n;
+                t.ldf = 2 * ld;
+                t.ldv = ld;
+                CK(cir_launch_tcf(t, St, c->stream, &nl));
             }
-            TcfArgs t;
-            memset(&t, 0, sizeof t);
-            t.F = F;
-            t.sF = (long long)n * 2 * ld;
-            t.m0 = M0;
-            t.sm0 = 9LL * ld;
-            t.mt = M + (size_t)kk * 9 * ld;
-            t.smt = (long long)kc * 9 * ld;
-            t.out = tcf + (size_t)k * 6;
-            t.sout = (long long)K * 6;
-            t.n = n;
-            t.ldf = 2 * ld;
-            t.ldv = ld;
-            CK(cir_launch_tcf(t, S, c->stream, &launches));
+            return CIR_OK;
+        };
+        if (p.cuda_graphs) {
+            const std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2);
+            GraphEntry *ge = nullptr;
+            for (auto &x : c->graphs)
+                if (x.key == key) ge = &x;
+            if (!ge) {
+                int nl = 0;
+                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                const int rc2 = run_steps(nl);
+                cudaGraph_t gr = nullptr;
+                const cudaError_t ce = cudaStreamEndCapture(c->stream, &gr);
+                if (rc2) {
+                    if (gr) cudaGraphDestroy(gr);
+                    return rc2;
+                }
+                if (ce != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "capturing the step loop: %s", cudaGetErrorString(ce));
+                GraphEntry ne;
+                ne.key = key;
+                ne.launches = nl;
+                const cudaError_t ie = cudaGraphInstantiate(&ne.exec, gr, 0);
+                cudaGraphDestroy(gr);
+                if (ie != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "instantiating the step loop: %s", cudaGetErrorString(ie));
+                if (c->graphs.size() >= 32) {
+                    cudaGraphExecDestroy(c->graphs.front().exec);
+                    c->graphs.erase(c->graphs.begin());
+                }
+                c->graphs.push_back(ne);
+                ge = &c->graphs.back();
+            }
+            CK(cudaGraphLaunch(ge->exec, c->stream));
+            launches += ge->launches;
+        } else {
+            int nl = 0;
+            if ((rc = run_steps(nl))) return rc;
+            launches += nl;
         }
         CK(cudaEventRecord(ev[4], c->stream));
         CK(cudaEventSynchronize(ev[4]));
@@ -712,19 +832,20 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
     cudaEventElapsedTime(&ms_total, ev[0], ev[7]);
     count_launch(c, launches);
     c->stats.frame_steps += steps;
+    if (ms_run) *ms_run = ms_total;
 
-    // ---------------- finishing steps (calcIR.cu:772-839) ----------------
-    std::vector<double> htcf((size_t)steps * 6), hipr(nomega), hmipr(nomega), hsw(nomega);
-    std::vector<unsigned long long> hcnt(nomega);
+    // results: correlation sums, histograms, spectral density of every trajectory
+    std::vector<double> htcf((size_t)steps * 6), hipr((size_t)T * nomega), hmipr((size_t)T * nomega), hsw((size_t)T * nomega);
+    std::vector<unsigned long long> hcnt((size_t)T * nomega), oor(T);
     std::vector<int> hst(nb);
-    unsigned long long oor = 0, sweeps = 0;
+    unsigned long long sweeps = 0;
     CK(cudaMemcpyAsync(htcf.data(), tcf, (size_t)steps * 48, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hcnt.data(), c->buf[B_HCNT].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hipr.data(), c->buf[B_HIPR].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hmipr.data(), c->buf[B_HMIPR].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hsw.data(), c->buf[B_SW].p, (size_t)nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hcnt.data(), c->buf[B_HCNT].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hipr.data(), c->buf[B_HIPR].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hmipr.data(), c->buf[B_HMIPR].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hsw.data(), c->buf[B_SW].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(hst.data(), c->buf[B_STATUS].p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&oor, c->buf[B_OOR].p, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(oor.data(), c->buf[B_OOR].p, (size_t)T * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&sweeps, c->buf[B_SWEEPS].p, 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->stats.eig_sweeps += (long long)sweeps;
@@ -732,43 +853,137 @@ extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *b
         if (hst[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached");
     if (p.precision != CIR_PREC_FP32 && (rc = check_kernel_flag(c))) return rc;
 
-    // sum over origins, T1 damping and 1/nsamples (calcIR.cu:777-782, 798-802, 815-819)
-    std::vector<double> damped[3];
-    for (int q = 0; q < 3; q++) damped[q].assign((size_t)2 * K, 0.0);
-    for (int k = 0; k < K; k++) {
-        double sum[6] = {0, 0, 0, 0, 0, 0};
-        for (int s = 0; s < S; s++)
-            for (int q = 0; q < 6; q++) sum[q] += htcf[((size_t)s * K + k) * 6 + q];
-        const double dcy = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
-        for (int q = 0; q < 3; q++) {
-            damped[q][2 * k] = sum[2 * q] * dcy;
-            damped[q][2 * k + 1] = sum[2 * q + 1] * dcy;
+    for (int tr = 0; tr < T; tr++) {
+        cir_result *r = res + tr;
+        const double *sw_t = hsw.data() + (size_t)tr * nomega, *ipr_t = hipr.data() + (size_t)tr * nomega,
+                     *mipr_t = hmipr.data() + (size_t)tr * nomega;
+        const unsigned long long *cnt_t = hcnt.data() + (size_t)tr * nomega;
+        // sum over origins, T1 damping and 1/nsamples (calcIR.cu:777-782, 798-802, 815-819)
+        std::vector<double> damped[3];
+        for (int q = 0; q < 3; q++) damped[q].assign((size_t)2 * K, 0.0);
+        for (int k = 0; k < K; k++) {
+            double sum[6] = {0, 0, 0, 0, 0, 0};
+            for (int s = tr * S; s < (tr + 1) * S; s++)
+                for (int q = 0; q < 6; q++) sum[q] += htcf[((size_t)s * K + k) * 6 + q];
+            const double dcy = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
+            for (int q = 0; q < 3; q++) {
+                damped[q][2 * k] = sum[2 * q] * dcy;
+                damped[q][2 * k + 1] = sum[2 * q + 1] * dcy;
+            }
         }
+        double *outs[3] = {r->tcf_ir, r->tcf_vv, r->tcf_vh};
+        for (int q = 0; q < 3; q++)
+            if (outs[q]) memcpy(outs[q], damped[q].data(), (size_t)2 * K * 8);
+        // spectral density and frequency distributions (calcIR.cu:831-839)
+        const float norm = (float)(n * S * K);
+        for (int i = 0; i < nomega; i++) {
+            if (r->omega) r->omega[i] = (float)(p.omegaStart + p.omegaStep * i);
+            if (r->sw) r->sw[i] = (float)(sw_t[i] / S);
+            const float pw = (float)((double)cnt_t[i] / p.omegaStep) / norm;
+            if (r->pw) r->pw[i] = pw;
+            if (r->rw) r->rw[i] = ((float)(ipr_t[i] / p.omegaStep) / norm) / pw;
+            if (r->rmw) r->rmw[i] = ((float)(mipr_t[i] / p.omegaStep) / norm) / pw;
+        }
+        // lineshapes (calcIR.cu:786-827, 890-919)
+        float *lsv[3] = {r->ls_ir, r->ls_vv, r->ls_vh};
+        int nls = 0;
+        for (int q = 0; q < 3; q++) {
+            std::vector<double> y;
+            int rc3 = c2r_dev(c, damped[q].data(), y);
+            if (rc3) return rc3;
+            nls = lineshape_rows(&p, y.data(), q == 0 ? r->ls_omega : nullptr, lsv[q]);
+        }
+        r->nls = nls;
+        r->bins_out_of_range = (long long)oor[tr];
+        r->frame_steps_per_s = ms_total > 0 ? steps / (ms_total * 1e-3) : 0.0;
     }
-    double *outs[3] = {r->tcf_ir, r->tcf_vv, r->tcf_vh};
-    for (int q = 0; q < 3; q++)
-        if (outs[q]) memcpy(outs[q], damped[q].data(), (size_t)2 * K * 8);
-    // spectral density and frequency distributions (calcIR.cu:831-839)
-    const float norm = (float)(n * S * K);
-    for (int i = 0; i < nomega; i++) {
-        if (r->omega) r->omega[i] = (float)(p.omegaStart + p.omegaStep * i);
-        if (r->sw) r->sw[i] = (float)(hsw[i] / S);
-        const float pw = (float)((double)hcnt[i] / p.omegaStep) / norm;
-        if (r->pw) r->pw[i] = pw;
-        if (r->rw) r->rw[i] = ((float)(hipr[i] / p.omegaStep) / norm) / pw;
-        if (r->rmw) r->rmw[i] = ((float)(hmipr[i] / p.omegaStep) / norm) / pw;
+    return CIR_OK;
+}
+
+extern "C" int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *box, const int *frame_of_step,
+                       cir_result *r) {
+    if (!c || !xyz || !box || !r || nframes < 1) return cir_fail(CIR_ERR_ARG, "cir_run: bad argument");
+    const cir_params &p = c->p;
+    const long long steps = (long long)p.nsamples * p.ntcfpoints;
+    std::vector<int> fidx(steps);
+    if (frame_of_step) {
+        for (long long i = 0; i < steps; i++) {
+            if (frame_of_step[i] < 0 || frame_of_step[i] >= nframes)
+                return cir_fail(CIR_ERR_ARG, "frame_of_step[%lld] = %d outside [0, %d)", i, frame_of_step[i], nframes);
+            fidx[i] = frame_of_step[i];
+        }
+    } else {
+        if (nframes != steps) return cir_fail(CIR_ERR_ARG, "cir_run: %d frames for %lld frame-steps", nframes, steps);
+        for (long long i = 0; i < steps; i++) fidx[i] = (int)i;
     }
-    // lineshapes (calcIR.cu:786-827, 890-919)
-    float *lsv[3] = {r->ls_ir, r->ls_vv, r->ls_vh};
-    int nls = 0;
-    for (int q = 0; q < 3; q++) {
-        std::vector<double> y;
-        int rc3 = c2r_dev(c, damped[q].data(), y);
-        if (rc3) return rc3;
-        nls = lineshape_rows(&p, y.data(), q == 0 ? r->ls_omega : nullptr, lsv[q]);
+    const size_t nx = (size_t)nframes * c->natoms * 3;
+    if (!is_device_ptr(xyz) && !all_finite(xyz, nx)) return cir_fail(CIR_ERR_NONFINITE, "positions contain NaN or Inf");
+    if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
+    void *dxyz, *dbox;
+    int rc;
+    if ((rc = stage_in(c, B_XYZ, xyz, nx * 4, &dxyz, true))) return rc;
+    if ((rc = stage_in(c, B_BOX, box, (size_t)nframes * 12, &dbox, true))) return rc;
+    return run_group(c, ctx_group(c), static_cast<const float *>(dxyz), static_cast<const float *>(dbox), fidx, r, nullptr);
+}
+
+extern "C" int cir_run_multi(cir_ctx *c, int ntraj, const cir_traj_in *traj, cir_result *results) {
+    if (!c || ntraj < 1 || !traj || !results) return cir_fail(CIR_ERR_ARG, "cir_run_multi: bad argument");
+    const cir_params &p = c->p;
+    const long long steps = (long long)p.nsamples * p.ntcfpoints;
+    // groups of equal size, in order of size
+    std::map<int, std::vector<int>> groups;
+    for (int i = 0; i < ntraj; i++) {
+        const cir_traj_in &t = traj[i];
+        if (!t.xyz || !t.box || t.nframes < 1) return cir_fail(CIR_ERR_ARG, "cir_run_multi: trajectory %d: bad argument", i);
+        if (t.natoms < p.natom_mol || t.natoms % p.natom_mol)
+            return cir_fail(CIR_ERR_ARG, "trajectory %d: natoms %d is not a positive multiple of natom_mol %d", i, t.natoms,
+                            p.natom_mol);
+        const int n = t.natoms / p.natom_mol * p.nchrom_mol;
+        if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "trajectory %d: %d chromophores exceed %d", i, n, cir_eigh_max_n());
+        if (!t.frame_of_step && t.nframes != steps)
+            return cir_fail(CIR_ERR_ARG, "trajectory %d: %d frames for %lld frame-steps", i, t.nframes, steps);
+        if (t.frame_of_step)
+            for (long long k = 0; k < steps; k++)
+                if (t.frame_of_step[k] < 0 || t.frame_of_step[k] >= t.nframes)
+                    return cir_fail(CIR_ERR_ARG, "trajectory %d: frame_of_step[%lld] = %d outside [0, %d)", i, k,
+                                    t.frame_of_step[k], t.nframes);
+        const size_t nx = (size_t)t.nframes * t.natoms * 3;
+        if (!is_device_ptr(t.xyz) && !all_finite(t.xyz, nx))
+            return cir_fail(CIR_ERR_NONFINITE, "trajectory %d: positions contain NaN or Inf", i);
+        if (!is_device_ptr(t.box) && !all_finite(t.box, 3 * (size_t)t.nframes))
+            return cir_fail(CIR_ERR_NONFINITE, "trajectory %d: box contains NaN or Inf", i);
+        groups[t.natoms].push_back(i);
     }
-    r->nls = nls;
-    r->bins_out_of_range = (long long)oor;
-    r->frame_steps_per_s = ms_total > 0 ? steps / (ms_total * 1e-3) : 0.0;
+    for (auto &kv : groups) {
+        const int natoms = kv.first;
+        const std::vector<int> &ids = kv.second;
+        Group g;
+        g.natoms = natoms;
+        g.nmol = natoms / p.natom_mol;
+        g.n = g.nmol * p.nchrom_mol;
+        g.ld = (g.n + 3) & ~3;
+        g.ntraj = (int)ids.size();
+        long long nf = 0;
+        for (int i : ids) nf += traj[i].nframes;
+        CK(c->buf[B_XYZ].ensure((size_t)nf * natoms * 12));
+        CK(c->buf[B_BOX].ensure((size_t)nf * 12));
+        std::vector<int> fidx((size_t)g.ntraj * steps);
+        long long off = 0;
+        for (int j = 0; j < g.ntraj; j++) {
+            const cir_traj_in &t = traj[ids[j]];
+            CK(cudaMemcpyAsync(c->buf[B_XYZ].as<float>() + (size_t)off * natoms * 3, t.xyz, (size_t)t.nframes * natoms * 12,
+                               cudaMemcpyDefault, c->stream));
+            CK(cudaMemcpyAsync(c->buf[B_BOX].as<float>() + (size_t)off * 3, t.box, (size_t)t.nframes * 12, cudaMemcpyDefault,
+                               c->stream));
+            for (long long k = 0; k < steps; k++)
+                fidx[(size_t)j * steps + k] = (int)(off + (t.frame_of_step ? t.frame_of_step[k] : k));
+            off += t.nframes;
+        }
+        std::vector<cir_result> rs(g.ntraj);
+        for (int j = 0; j < g.ntraj; j++) rs[j] = results[ids[j]];
+        const int rc = run_group(c, g, c->buf[B_XYZ].as<float>(), c->buf[B_BOX].as<float>(), fidx, rs.data(), nullptr);
+        if (rc) return rc;
+        for (int j = 0; j < g.ntraj; j++) results[ids[j]] = rs[j];
+    }
     return CIR_OK;
 }

@@ -67,6 +67,8 @@ struct EighArgs {
     int *status;          // [nmat] 0 ok, 1 sweep cap reached
     unsigned long long *sweeps;   // accumulated QR sweeps (may be null)
     // frequency distribution (calcIR.cu:493-538); hist_count == null disables it
+    int hist_group;       // matrices per histogram set (consecutive matrices; 0: one set for all);
+                          // set g uses hist_*[g*nomega ..] and out_of_range[g]
     unsigned long long *hist_count;
     double *hist_ipr, *hist_mipr;
     unsigned long long *out_of_range;
@@ -102,7 +104,9 @@ struct GemmArgs {
     float dt_over_hbar;
     int *err;              // tensor-core kernels: set to 1 when a bounded wait gives up
 };
-cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches);
+// SIMT tile shapes: 128 x 128 x 8, or 64 x 64 x 16 (more blocks for small products)
+constexpr int CIR_GEMM_TILE_128 = 0, CIR_GEMM_TILE_64 = 1;
+cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches, int tile = CIR_GEMM_TILE_128);
 // the same product on the tensor cores (tcgen05), precision CIR_PREC_TF32
 cudaError_t cir_launch_tc_gemm(const GemmArgs &g, int batch, int precision, cudaStream_t s, int *launches);
 size_t cir_tc_gemm_smem_bytes();

@@ -84,6 +84,8 @@ extern "C" int cir_params_default(cir_params *p) {
     p->precision = CIR_PREC_FP32;
     p->batch_frames = 0;
     p->verbose = 0;
+    p->cuda_graphs = 1;
+    p->autotune = 1;
     return CIR_OK;
 }
 
@@ -159,6 +161,8 @@ extern "C" int cir_params_parse_file(const char *path, cir_params *p) {
         else if (!strcmp(k, "synth_sigma_rot")) scan_float(v, &p->synth_sigma_rot);
         else if (!strcmp(k, "batch_frames")) scan_int(v, &p->batch_frames);
         else if (!strcmp(k, "verbose")) scan_int(v, &p->verbose);
+        else if (!strcmp(k, "cuda_graphs")) scan_int(v, &p->cuda_graphs);
+        else if (!strcmp(k, "autotune")) scan_int(v, &p->autotune);
         else if (!strcmp(k, "precision")) {
             if (!strcmp(v, "fp32")) p->precision = CIR_PREC_FP32;
             else if (!strcmp(v, "tf32")) p->precision = CIR_PREC_TF32;

@@ -480,12 +480,13 @@ __global__ void __launch_bounds__(256) k_dc_finish(EighArgs a) {
         if (lane == 0) {
             const float wi = dw[j] + a.avef;
             const int bin = (int)roundf((wi - a.omegaStart) / (float)a.omegaStep);
+            const size_t grp = a.hist_group > 0 ? (size_t)(mat / a.hist_group) : 0;
             if (bin >= 0 && bin < a.nomega) {
-                atomicAdd(a.hist_count + bin, 1ull);
-                atomicAdd(a.hist_ipr + bin, (double)(1.f / s4));
-                atomicAdd(a.hist_mipr + bin, (double)(1.f / m4));
+                atomicAdd(a.hist_count + grp * a.nomega + bin, 1ull);
+                atomicAdd(a.hist_ipr + grp * a.nomega + bin, (double)(1.f / s4));
+                atomicAdd(a.hist_mipr + grp * a.nomega + bin, (double)(1.f / m4));
             } else {
-                atomicAdd(a.out_of_range, 1ull);
+                atomicAdd(a.out_of_range + grp, 1ull);
             }
         }
     }

@@ -5,20 +5,28 @@
 // is two real GEMMs, 8 N^3 flops:
 //     G  = V^T F                  (epilogue: row j of G times exp(+i w_j dt/hbar))
 //     F' = V G
-// 128x128x8 block tiles, 256 threads, 8x8 outputs per thread, double-buffered shared
-// memory; edges are predicated so any N works.
+// 128x128x8 or 64x64x16 block tiles, 256 threads, 8x8 or 4x4 outputs per thread,
+// double-buffered shared memory; edges are predicated so any N works.
 #include "cir_device.cuh"
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 8, TM = 8, TN = 8;
+// Tile shapes (256 threads, a 16 x 16 thread grid, TM x TN outputs per thread in 4 x 4 groups
+// 64 rows / columns apart): 128 x 128 x 8 for large products, 64 x 64 x 16 for products
+// whose 128 x 128 grid would not fill the SMs.  The autotuner of the library picks one.
+template <int BM_, int BN_, int BK_>
+struct Tile {
+    static constexpr int BM = BM_, BN = BN_, BK = BK_, TM = BM_ / 16, TN = BN_ / 16;
+};
+using TileL = Tile<128, 128, 8>;
+using TileS = Tile<64, 64, 16>;
 constexpr int GT = 256;
 
-template <bool ACOL>
+template <class T, bool ACOL>
 __device__ __forceinline__ void load_a(const GemmArgs &g, const float *A, int m0, int k0, float (&ra)[4]) {
     const int t = threadIdx.x;
     if (ACOL) {   // element (i, k) at A[k*lda + i]; thread loads 4 consecutive i of one k
-        const int kk = t / (BM / 4), i = (t % (BM / 4)) * 4;
+        const int kk = t / (T::BM / 4), i = (t % (T::BM / 4)) * 4;
         const int gk = k0 + kk, gi = m0 + i;
         const float *p = A + (size_t)gk * g.lda + gi;
         if (gk < g.K && gi + 3 < g.M && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
@@ -29,7 +37,7 @@ __device__ __forceinline__ void load_a(const GemmArgs &g, const float *A, int m0
             for (int q = 0; q < 4; q++) ra[q] = (gk < g.K && gi + q < g.M) ? p[q] : 0.f;
         }
     } else {      // element (i, k) at A[i*lda + k]; thread loads 4 consecutive k of one i
-        const int i = t / 2, kk = (t % 2) * 4;
+        const int i = t / (T::BK / 4), kk = (t % (T::BK / 4)) * 4;
         const int gi = m0 + i, gk = k0 + kk;
         const float *p = A + (size_t)gi * g.lda + gk;
         if (gi < g.M && gk + 3 < g.K && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
@@ -42,22 +50,23 @@ __device__ __forceinline__ void load_a(const GemmArgs &g, const float *A, int m0
     }
 }
 
-template <bool ACOL>
-__device__ __forceinline__ void store_a(float (*As)[BM], const float (&ra)[4]) {
+template <class T, bool ACOL>
+__device__ __forceinline__ void store_a(float (*As)[T::BM], const float (&ra)[4]) {
     const int t = threadIdx.x;
     if (ACOL) {
-        const int kk = t / (BM / 4), i = (t % (BM / 4)) * 4;
+        const int kk = t / (T::BM / 4), i = (t % (T::BM / 4)) * 4;
         *reinterpret_cast<float4 *>(&As[kk][i]) = make_float4(ra[0], ra[1], ra[2], ra[3]);
     } else {
-        const int i = t / 2, kk = (t % 2) * 4;
+        const int i = t / (T::BK / 4), kk = (t % (T::BK / 4)) * 4;
         #pragma unroll
         for (int q = 0; q < 4; q++) As[kk + q][i] = ra[q];
     }
 }
 
+template <class T>
 __device__ __forceinline__ void load_b(const GemmArgs &g, const float *B, int k0, int n0, float (&rb)[4]) {
     const int t = threadIdx.x;
-    const int kk = t / (BN / 4), j = (t % (BN / 4)) * 4;
+    const int kk = t / (T::BN / 4), j = (t % (T::BN / 4)) * 4;
     const int gk = k0 + kk, gj = n0 + j;
     const float *p = B + (size_t)gk * g.ldb + gj;
     if (gk < g.K && gj + 3 < g.N && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
@@ -69,8 +78,9 @@ __device__ __forceinline__ void load_b(const GemmArgs &g, const float *B, int k0
     }
 }
 
-template <bool ACOL>
+template <class T, bool ACOL>
 __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
+    constexpr int BM = T::BM, BN = T::BN, BK = T::BK, TM = T::TM, TN = T::TN;
     __shared__ __align__(16) float As[2][BK][BM];
     __shared__ __align__(16) float Bs[2][BK][BN];
     const int bz = blockIdx.z;
@@ -87,9 +97,9 @@ __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
         for (int j = 0; j < TN; j++) acc[i][j] = 0.f;
 
     float ra[4], rb[4];
-    load_a<ACOL>(g, A, m0, 0, ra);
-    load_b(g, B, 0, n0, rb);
-    store_a<ACOL>(As[0], ra);
+    load_a<T, ACOL>(g, A, m0, 0, ra);
+    load_b<T>(g, B, 0, n0, rb);
+    store_a<T, ACOL>(As[0], ra);
     {
         const int kk = threadIdx.x / (BN / 4), j = (threadIdx.x % (BN / 4)) * 4;
         *reinterpret_cast<float4 *>(&Bs[0][kk][j]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
@@ -99,37 +109,39 @@ __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
     for (int k0 = 0; k0 < g.K; k0 += BK) {
         const bool more = k0 + BK < g.K;
         if (more) {
-            load_a<ACOL>(g, A, m0, k0 + BK, ra);
-            load_b(g, B, k0 + BK, n0, rb);
+            load_a<T, ACOL>(g, A, m0, k0 + BK, ra);
+            load_b<T>(g, B, k0 + BK, n0, rb);
         }
         #pragma unroll
         for (int kk = 0; kk < BK; kk++) {
             float af[TM], bf[TN];
-            const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
-            const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4 + 64]);
-            const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
-            const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4 + 64]);
-            af[0] = a0.x; af[1] = a0.y; af[2] = a0.z; af[3] = a0.w;
-            af[4] = a1.x; af[5] = a1.y; af[6] = a1.z; af[7] = a1.w;
-            bf[0] = b0.x; bf[1] = b0.y; bf[2] = b0.z; bf[3] = b0.w;
-            bf[4] = b1.x; bf[5] = b1.y; bf[6] = b1.z; bf[7] = b1.w;
+            #pragma unroll
+            for (int q = 0; q < TM / 4; q++) {
+                const float4 a4 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4 + 64 * q]);
+                af[4 * q] = a4.x; af[4 * q + 1] = a4.y; af[4 * q + 2] = a4.z; af[4 * q + 3] = a4.w;
+            }
+            #pragma unroll
+            for (int q = 0; q < TN / 4; q++) {
+                const float4 b4 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4 + 64 * q]);
+                bf[4 * q] = b4.x; bf[4 * q + 1] = b4.y; bf[4 * q + 2] = b4.z; bf[4 * q + 3] = b4.w;
+            }
             #pragma unroll
             for (int i = 0; i < TM; i++)
                 #pragma unroll
                 for (int j = 0; j < TN; j++) acc[i][j] = fmaf(af[i], bf[j], acc[i][j]);
         }
         if (more) {
-            store_a<ACOL>(As[buf ^ 1], ra);
+            store_a<T, ACOL>(As[buf ^ 1], ra);
             const int kk = threadIdx.x / (BN / 4), j = (threadIdx.x % (BN / 4)) * 4;
             *reinterpret_cast<float4 *>(&Bs[buf ^ 1][kk][j]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
         }
         __syncthreads();
         buf ^= 1;
     }
-    // rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns tx*4 + {0..3} and 64 + tx*4 + {0..3}
+    // rows ty*4 + {0..3} (+ 64); columns tx*4 + {0..3} (+ 64)
     #pragma unroll
     for (int i = 0; i < TM; i++) {
-        const int r = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+        const int r = m0 + 64 * (i / 4) + ty * 4 + (i % 4);
         if (r >= g.M) continue;
         float cph = 1.f, sph = 0.f;
         if (g.epilogue == 1) {
@@ -137,7 +149,7 @@ __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
             sincosf(ph, &sph, &cph);
         }
         #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < TN / 4; h++) {
             const int c = n0 + h * 64 + tx * 4;
             float v[4] = {acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]};
             if (g.epilogue == 1) {   // (re, im) pairs times exp(+i ph)
@@ -166,15 +178,22 @@ __global__ void k_identity(float *F, int n, int ldf, long long sF) {
     for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) f[(size_t)r * ldf + c] = (c == 2 * r) ? 1.f : 0.f;
 }
 
+template <class T>
+cudaError_t launch_sgemm(const GemmArgs &g, int batch, cudaStream_t s) {
+    dim3 grid((g.N + T::BN - 1) / T::BN, (g.M + T::BM - 1) / T::BM, batch);
+    if (g.a_colmajor) k_sgemm<T, true><<<grid, GT, 0, s>>>(g);
+    else k_sgemm<T, false><<<grid, GT, 0, s>>>(g);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
-cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches) {
+cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches, int tile) {
     if (g.epilogue == 1 && (g.N & 1)) return cudaErrorInvalidValue;
-    dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, batch);
-    if (g.a_colmajor) k_sgemm<true><<<grid, GT, 0, s>>>(g);
-    else k_sgemm<false><<<grid, GT, 0, s>>>(g);
+    if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
+    const cudaError_t e = tile == CIR_GEMM_TILE_64 ? launch_sgemm<TileS>(g, batch, s) : launch_sgemm<TileL>(g, batch, s);
     if (launches) *launches += 1;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t cir_launch_identity(float *F, int n, int ldf, long long sF, int batch, cudaStream_t s, int *launches) {

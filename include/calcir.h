@@ -87,6 +87,8 @@ typedef struct cir_params {
     int   precision;               /* CIR_PREC_*                                       */
     int   batch_frames;            /* frame-steps per eigensolver batch, 0 = automatic */
     int   verbose;                 /* 0 silent, 1 reference-style progress on stdout   */
+    int   cuda_graphs;             /* 1: replay the per-step launches from captured CUDA graphs */
+    int   autotune;                /* 1: time the GEMM tile shapes once per problem shape      */
 } cir_params;
 
 /* Whole-job results, caller-owned host arrays sized by cir_result_sizes. */
@@ -219,6 +221,24 @@ int cir_lineshape(cir_ctx *c, const double *tcf, float *omega, float *intensity,
  * Replaces the sample/frame loops and the finishing steps of main (calcIR.cu:360-839). */
 int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *box,
             const int *frame_of_step, cir_result *r);
+
+/* One trajectory of a multi-trajectory job. */
+typedef struct cir_traj_in {
+    int          natoms;          /* its own system size (a multiple of natom_mol)           */
+    int          nframes;
+    const float *xyz;             /* [nframes][natoms][3] nm, host or device                  */
+    const float *box;             /* [nframes][3]                                             */
+    const int   *frame_of_step;   /* [nsamples*ntcfpoints], or NULL for the identity           */
+} cir_traj_in;
+
+/* Many independent trajectories, boxes of uneven size allowed, with the context's
+ * parameters (its own natoms is not used): trajectories of equal size are batched through
+ * every launch (their eigensolves, propagation steps and contractions share launches), the
+ * per-step launches are replayed from captured CUDA graphs (cuda_graphs) and the SIMT GEMM
+ * tile shapes come from the autotuner (autotune).  results[i] receives trajectory i's
+ * outputs exactly as cir_run would fill them.  No counterpart in the reference, which runs
+ * one trajectory per process (calcIR.cu:360-839 per run). */
+int cir_run_multi(cir_ctx *c, int ntraj, const cir_traj_in *traj, cir_result *results);
 
 #ifdef __cplusplus
 }
