@@ -111,6 +111,7 @@ SIGNATURES = {
     "cir_lineshape": [P, P, P, P, C.POINTER(C.c_int)],
     "cir_run": [P, C.c_int, P, P, P, C.POINTER(Result)],
     "cir_run_multi": [P, C.c_int, C.POINTER(TrajIn), C.POINTER(Result)],
+    "cir_xtc_write": [C.c_char_p, C.c_int, C.c_int, P, P, P, C.c_float],
 }
 _RESTYPE = {"cir_version": C.c_char_p, "cir_last_error": C.c_char_p}
 

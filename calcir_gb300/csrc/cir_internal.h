@@ -33,4 +33,10 @@ struct CirMaps {
 // Fills m for imap 0/1 and ispecies 0..3; returns false for any other imap.
 bool cir_maps(int imap, int ispecies, CirMaps *m);
 
+
+// .xtc trajectories (host_xtc.cpp), reached through cir_traj_info / cir_traj_read
+bool cir_is_xtc(const char *path);
+int cir_xtc_info(const char *path, int *natoms, int *nframes, float *frame_dt);
+int cir_xtc_read(const char *path, int first, int count, float *xyz, float *boxes, float *times);
+
 #endif

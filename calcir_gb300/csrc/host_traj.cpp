@@ -2,8 +2,9 @@
 // executable for user-supplied positions.  Layout (little endian):
 //   char magic[8] = "CIRTRJ01"; int32 natoms; int32 nframes; float32 frame_dt; int32 0;
 //   per frame: float32 time; float32 box[3]; float32 xyz[natoms][3]   (nm, ps)
-// Stands in for the xtc calls read_xtc_natoms / read_xtc_n_frames / xdr_seek / read_xtc
-// (calcIR.cu:212-223, 341-352, 376-395).
+// cir_traj_info / cir_traj_read also read GROMACS .xtc files (detected by their magic
+// number, host_xtc.cpp); together they stand in for read_xtc_natoms / read_xtc_n_frames /
+// xdr_seek / read_xtc (calcIR.cu:212-223, 341-352, 376-395).
 #include "cir_internal.h"
 
 #include <cstdio>
@@ -41,6 +42,7 @@ static FILE *open_checked(const char *path, int32_t hdr[4]) {
 }
 
 extern "C" int cir_traj_info(const char *path, int *natoms, int *nframes, float *frame_dt) {
+    if (path && cir_is_xtc(path)) return cir_xtc_info(path, natoms, nframes, frame_dt);
     int32_t hdr[4];
     FILE *f = path ? open_checked(path, hdr) : nullptr;
     if (!f) return cir_fail(CIR_ERR_IO, "WARNING: The file %s could not be opened as a CIRTRJ01 trajectory.", path ? path : "(null)");
@@ -52,6 +54,7 @@ extern "C" int cir_traj_info(const char *path, int *natoms, int *nframes, float 
 }
 
 extern "C" int cir_traj_read(const char *path, int first, int count, float *xyz, float *boxes, float *times) {
+    if (path && cir_is_xtc(path)) return cir_xtc_read(path, first, count, xyz, boxes, times);
     int32_t hdr[4];
     FILE *f = path ? open_checked(path, hdr) : nullptr;
     if (!f) return cir_fail(CIR_ERR_IO, "cannot open %s as a CIRTRJ01 trajectory", path ? path : "(null)");

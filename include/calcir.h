@@ -151,7 +151,14 @@ int cir_traj_write(const char *path, int natoms, int nframes, float frame_dt,
                    const float *times, const float *boxes, const float *xyz);
 int cir_traj_info(const char *path, int *natoms, int *nframes, float *frame_dt); /* read_xtc_natoms calcIR.cu:212 */
 int cir_traj_read(const char *path, int first, int count, float *xyz, float *boxes,
-                  float *times);                                /* xdr_seek + read_xtc calcIR.cu:380-390 */
+                  float *times);
+
+/* Writes a GROMACS .xtc trajectory (XDR, compressed coordinates at `precision` per nm, e.g.
+ * 1000): boxes [nframes][3] (diagonal), times [nframes] ps (NULL: 0).  cir_traj_info and
+ * cir_traj_read read .xtc files as well as CIRTRJ01 ones, so the drop-in executable takes
+ * `xtcf traj.xtc` like the reference (which reads through libxdrfile, calcIR.cu:212-223). */
+int cir_xtc_write(const char *path, int natoms, int nframes, const float *xyz, const float *boxes,
+                  const float *times, float precision);                                /* xdr_seek + read_xtc calcIR.cu:380-390 */
 
 /* ---------------- engine ---------------- */
 int cir_create(const cir_params *p, int natoms, cir_ctx **out); /* allocations + magma_init calcIR.cu:230-319 */

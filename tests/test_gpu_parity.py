@@ -234,6 +234,37 @@ def test_dropin_executable(lib, tmp_path):
     assert r.returncode != 0 and "Usage" in r.stdout
 
 
+def test_dropin_executable_reads_xtc(lib, tmp_path):
+    """`xtcf traj.xtc` (a GROMACS trajectory, 1/1000 nm precision): the executable's spectra
+    equal a run on the frames as decoded, and stay within the quantisation of the
+    positions of the uncompressed run."""
+    import ctypes as C
+    meta, _ = load_golden("hod_d2o")
+    xyz, box = lib.synth_trajectory(meta["nmol"], meta["nframes"], seed=meta["seed"])
+    b = np.ascontiguousarray(np.broadcast_to(box, (xyz.shape[0], 3)), np.float32)
+    t = (0.010 * np.arange(xyz.shape[0])).astype(np.float32)
+    from calcir_gb300._lib import check, load
+    check(load().cir_xtc_write(str(tmp_path / "traj.xtc").encode(), xyz.shape[1], xyz.shape[0],
+                               C.c_void_p(xyz.ctypes.data), C.c_void_p(b.ctypes.data), C.c_void_p(t.ctypes.data),
+                               C.c_float(1000.0)))
+    lines = ["xtcf traj.xtc", "outf x", "natom_mol 4"] + [f"{k} {v}" for k, v in meta["keys"].items()]
+    (tmp_path / "input.inp").write_text("\n".join(lines) + "\n")
+    r = subprocess.run([lib.EXE_PATH, "input.inp"], cwd=tmp_path, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+    dec = np.zeros_like(xyz)
+    check(load().cir_traj_read(str(tmp_path / "traj.xtc").encode(), 0, xyz.shape[0], C.c_void_p(dec.ctypes.data),
+                               None, None))
+    assert np.abs(dec - xyz).max() <= 0.5e-3 + 1e-6
+    prm, _, _, fos = _frames_for(lib, meta)
+    with lib.Engine(make_params(lib, prm), xyz.shape[1]) as eng:
+        out = eng.run(dec, box, fos)
+    for f, k in (("irrtcf", "tcf_ir"), ("vvrtcf", "tcf_vv"), ("spdn", "sw")):
+        a = np.loadtxt(tmp_path / f"x_{f}.dat", ndmin=2)[:, 1]
+        ref = out[k].real if k.startswith("tcf") else out[k]
+        assert O.rel_l2(a, ref) < 1e-5, f
+
+
 @pytest.mark.parametrize("nmol", [512, 1024])
 def test_full_size_eigen_and_unitarity(lib, nmol):
     """Full-size systems (1024 / 2048 chromophores): eigen-residuals, orthogonality, and
