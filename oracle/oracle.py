@@ -99,12 +99,13 @@ def field_projection(xyz, box, natom_mol=4, nchrom_mol=2, imodel=1):
     return np.einsum("ck,ck->c", E, u)
 
 
-def hamiltonian(xyz, box, eproj, avef, natom_mol=4, nchrom_mol=2, ispecies=0, imap=0):
+def hamiltonian(xyz, box, eproj, avef, natom_mol=4, nchrom_mol=2, ispecies=0, imap=0, mp=None):
     """Exciton Hamiltonian, dipoles and polarisabilities: get_kappa_GPU, calcIR.cu:1176-1406.
 
-    Returns H (N, N), dip (3, N) and pol (6, N) in the order xx, yy, zz, xy, yz, zx."""
+    Returns H (N, N), dip (3, N) and pol (6, N) in the order xx, yy, zz, xy, yz, zx.
+    ``mp`` overrides the map coefficients (a dict like ``maps`` returns)."""
     box = np.asarray(box, np.float64)
-    mp = maps(imap, ispecies)
+    mp = maps(imap, ispecies) if mp is None else mp
     mol, n, Hpos, Opos, u = chromophores(xyz, box, natom_mol, nchrom_mol)
     E = np.asarray(eproj, np.float64)
     w = mp["w"][0] + mp["w"][1] * E + mp["w"][2] * E * E          # calcIR.cu:1256
@@ -136,11 +137,11 @@ def hamiltonian(xyz, box, eproj, avef, natom_mol=4, nchrom_mol=2, ispecies=0, im
     return H, dip, pol
 
 
-def frame(xyz, box, prm: dict):
+def frame(xyz, box, prm: dict, mp=None):
     """Field, Hamiltonian, dipoles and polarisabilities of one frame."""
     E = field_projection(xyz, box, prm["natom_mol"], prm["nchrom_mol"], prm["imodel"])
     H, dip, pol = hamiltonian(xyz, box, E, prm["avef"], prm["natom_mol"], prm["nchrom_mol"],
-                              prm["ispecies"], prm["map"])
+                              prm["ispecies"], prm["map"], mp)
     return E, H, dip, pol
 
 
@@ -191,7 +192,7 @@ def lineshape_rows(prm, y):
     return np.array(om), np.array(val)
 
 
-def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=False):
+def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=False, mp=None):
     """The whole job (main, calcIR.cu:360-839) in FP64.
 
     frames[f] is the (natoms, 3) position array of frame f, boxes[f] its box diagonal;
@@ -216,7 +217,7 @@ def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=Fa
     for s in range(S):
         for k in range(K):
             f = frame_of_step[s * K + k]
-            E, H, dip, pol = frame(frames[f], boxes[f], prm)
+            E, H, dip, pol = frame(frames[f], boxes[f], prm, mp)
             N = H.shape[0]
             lam, V = np.linalg.eigh(H)
             mvec = np.vstack([dip, pol])
