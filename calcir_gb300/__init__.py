@@ -261,6 +261,31 @@ class Engine:
         check(self.lib.cir_run(self.h, nf, ptr(xyz), ptr(boxes), ptr(fos), C.byref(r)))
         return _result_dict(bufs, r)
 
+    def get_coeffs(self) -> np.ndarray:
+        """The 13 map and coupling coefficients (w0 w1 w2 x0 x1 p0 p1 mup0 mup1 mup2 wi0 wi1 wi2)."""
+        t = np.zeros(13, np.float32)
+        check(self.lib.cir_get_coeffs(self.h, ptr(t)))
+        return t
+
+    def set_coeffs(self, theta) -> None:
+        t = np.ascontiguousarray(theta, np.float32)
+        check(self.lib.cir_set_coeffs(self.h, ptr(t)))
+
+    def loss_grad(self, xyz, boxes, frame_of_step, target_ir, target_vv) -> tuple[float, np.ndarray]:
+        """(L, dL/dtheta) of L = sum (ls_ir - target_ir)^2 + (ls_vv - target_vv)^2 over the printed
+        lineshape rows (cir_loss_grad, the adjoint through propagation and eigendecomposition)."""
+        xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, self.natoms, 3)
+        nf = xyz.shape[0]
+        boxes = np.ascontiguousarray(np.broadcast_to(np.asarray(boxes, np.float32), (nf, 3)))
+        fos = None if frame_of_step is None else np.ascontiguousarray(frame_of_step, np.int32)
+        ti = np.ascontiguousarray(target_ir, np.float32)
+        tv = np.ascontiguousarray(target_vv, np.float32)
+        loss = C.c_double()
+        grad = np.zeros(13, np.float64)
+        check(self.lib.cir_loss_grad(self.h, nf, ptr(xyz), ptr(boxes), ptr(fos), ptr(ti), ptr(tv), len(ti),
+                                     C.byref(loss), ptr(grad)))
+        return loss.value, grad
+
     def run_multi(self, trajectories) -> list[dict]:
         """Many trajectories, boxes of uneven size allowed (cir_run_multi): ``trajectories``
         is a list of (xyz (nframes, natoms, 3), boxes (nframes, 3) or (3,), frame_of_step or

@@ -112,6 +112,9 @@ SIGNATURES = {
     "cir_run": [P, C.c_int, P, P, P, C.POINTER(Result)],
     "cir_run_multi": [P, C.c_int, C.POINTER(TrajIn), C.POINTER(Result)],
     "cir_xtc_write": [C.c_char_p, C.c_int, C.c_int, P, P, P, C.c_float],
+    "cir_get_coeffs": [P, P],
+    "cir_set_coeffs": [P, P],
+    "cir_loss_grad": [P, C.c_int, P, P, P, P, P, C.c_int, P, P],
 }
 _RESTYPE = {"cir_version": C.c_char_p, "cir_last_error": C.c_char_p}
 

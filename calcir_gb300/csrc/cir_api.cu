@@ -52,6 +52,7 @@ enum {
     B_A, B_W, B_M, B_F, B_G, B_M0,                 // run: matrices
     B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
     B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR, B_DC, B_TUNE,
+    B_PSI, B_LAM, B_PA, B_PB, B_SEG, B_CKPT, B_R, B_T, B_GRAD,   // differentiation form
     B_COUNT
 };
 
@@ -985,5 +986,312 @@ extern "C" int cir_run_multi(cir_ctx *c, int ntraj, const cir_traj_in *traj, cir
         if (rc) return rc;
         for (int j = 0; j < g.ntraj; j++) results[ids[j]] = rs[j];
     }
+    return CIR_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Differentiation form: the gradient of a spectrum-mismatch loss with respect to the map and
+// coupling coefficients, by the adjoint of the propagation and of the eigendecomposition.
+// ---------------------------------------------------------------------------------------
+
+extern "C" int cir_get_coeffs(cir_ctx *c, float *theta) {
+    if (!c || !theta) return cir_fail(CIR_ERR_ARG, "cir_get_coeffs: bad argument");
+    const CirMaps &m = c->maps;
+    const float v[CIR_NTHETA] = {m.w[0], m.w[1], m.w[2], m.x[0], m.x[1], m.p[0], m.p[1],
+                                 m.mup[0], m.mup[1], m.mup[2], m.wi[0], m.wi[1], m.wi[2]};
+    memcpy(theta, v, sizeof v);
+    return CIR_OK;
+}
+
+extern "C" int cir_set_coeffs(cir_ctx *c, const float *t) {
+    if (!c || !t) return cir_fail(CIR_ERR_ARG, "cir_set_coeffs: bad argument");
+    for (int q = 0; q < CIR_NTHETA; q++)
+        if (!std::isfinite(t[q])) return cir_fail(CIR_ERR_NONFINITE, "cir_set_coeffs: coefficient %d is not finite", q);
+    CirMaps &m = c->maps;
+    m.w[0] = t[0]; m.w[1] = t[1]; m.w[2] = t[2];
+    m.x[0] = t[3]; m.x[1] = t[4];
+    m.p[0] = t[5]; m.p[1] = t[6];
+    m.mup[0] = t[7]; m.mup[1] = t[8]; m.mup[2] = t[9];
+    m.wi[0] = t[10]; m.wi[1] = t[11]; m.wi[2] = t[12];
+    return CIR_OK;
+}
+
+// Positions in the C2R output of the printed lineshape rows (the selection of lineshape_rows),
+// and the intensity normalisation.
+static std::vector<int> lineshape_index(const cir_params *p, float *norm_out) {
+    const int n = p->ntcfpoints + p->nzeros;
+    const float factor = (float)(2 * CIR_PI * CIR_HBAR / (p->dt * (float)n));
+    *norm_out = factor * (float)n;
+    std::vector<int> idx;
+    for (int i = n / 2; i < n; i++)
+        if (-1 * (i - p->ntcfpoints - p->nzeros) * factor + p->avef <= (float)p->omegaStop) idx.push_back(i);
+    for (int i = 0; i < p->ntcfpoints + p->nzeros / 2; i++)
+        if (-1 * i * factor + p->avef >= (float)p->omegaStart) idx.push_back(i);
+    return idx;
+}
+
+// x <- V_k exp(i L_k dt/hbar) V_k^T x for S origins, x n x 9 complex (row-major, 18 floats per
+// row); FP32 SIMT GEMMs.  V: origin s at V + s*sV, w likewise; tmp: S x n x 18.
+static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long long sV, const float *w, long long sw,
+                         float dt, float *x, float *tmp, int &launches) {
+    GemmArgs g1{};
+    g1.A = V; g1.lda = ld; g1.sA = sV; g1.a_colmajor = false;        // V^T (row-major view of V)
+    g1.B = x; g1.ldb = CIR_PSI_LD; g1.sB = (long long)n * CIR_PSI_LD;
+    g1.C = tmp; g1.ldc = CIR_PSI_LD; g1.sC = (long long)n * CIR_PSI_LD;
+    g1.M = n; g1.N = CIR_PSI_LD; g1.K = n;
+    g1.epilogue = 1; g1.w = w; g1.wstride = (int)sw;
+    g1.dt_over_hbar = (float)(dt / CIR_HBAR);
+    GemmArgs g2 = g1;
+    g2.a_colmajor = true;                                              // V itself
+    g2.B = tmp; g2.C = x; g2.epilogue = 0;
+    CK(cir_launch_gemm(g1, S, c->stream, &launches));
+    CK(cir_launch_gemm(g2, S, c->stream, &launches));
+    return CIR_OK;
+}
+
+// psi is checkpointed every CKPT steps (psi(0), then psi(j*CKPT - 1)); the backward pass
+// recomputes one segment of CKPT steps at a time from its checkpoint.
+constexpr int CKPT = 16;
+
+extern "C" int cir_loss_grad(cir_ctx *c, int nframes, const float *xyz, const float *box, const int *frame_of_step,
+                             const float *target_ir, const float *target_vv, int nls, double *loss, double *grad) {
+    if (!c || !xyz || !box || !target_ir || !target_vv || !loss || !grad || nframes < 1)
+        return cir_fail(CIR_ERR_ARG, "cir_loss_grad: bad argument");
+    const cir_params &p = c->p;
+    const int S = p.nsamples, K = p.ntcfpoints, n = c->n, ld = c->ld;
+    const long long steps = (long long)S * K;
+    float norm = 0.f;
+    const std::vector<int> rows = lineshape_index(&p, &norm);
+    if (nls != (int)rows.size())
+        return cir_fail(CIR_ERR_ARG, "cir_loss_grad: %d target rows, the lineshape has %zu", nls, rows.size());
+    std::vector<int> fidx(steps);
+    for (long long i = 0; i < steps; i++) {
+        const int f = frame_of_step ? frame_of_step[i] : (int)i;
+        if (f < 0 || f >= nframes) return cir_fail(CIR_ERR_ARG, "frame_of_step[%lld] = %d outside [0, %d)", i, f, nframes);
+        fidx[i] = f;
+    }
+    const size_t nx = (size_t)nframes * c->natoms * 3;
+    if (!is_device_ptr(xyz) && !all_finite(xyz, nx)) return cir_fail(CIR_ERR_NONFINITE, "positions contain NaN or Inf");
+    if (!is_device_ptr(box) && !all_finite(box, 3 * (size_t)nframes)) return cir_fail(CIR_ERR_NONFINITE, "box contains NaN or Inf");
+    // every frame-step of the job stays resident (one chunk)
+    const long long mstride = (long long)n * ld;
+    const size_t per_step = (size_t)2 * mstride * 4 + cir_dc_bytes(n, ld) + cir_eigh_de_bytes(ld) +
+                            (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)c->natoms * 12 + 64;
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess && per_step * steps > freeb / 2)
+        return cir_fail(CIR_ERR_NOMEM, "cir_loss_grad: %lld frame-steps need %.1f GB (half the free memory: %.1f GB)",
+                        steps, per_step * steps / 1e9, freeb / 2e9);
+    if (steps > 65535) return cir_fail(CIR_ERR_ARG, "cir_loss_grad: %lld frame-steps (at most 65535)", steps);
+    void *dxyz, *dbox;
+    int rc;
+    if ((rc = stage_in(c, B_XYZ, xyz, nx * 4, &dxyz, true))) return rc;
+    if ((rc = stage_in(c, B_BOX, box, (size_t)nframes * 12, &dbox, true))) return rc;
+    const int nb = (int)steps;
+    const size_t psz = (size_t)S * n * CIR_PSI_LD;            // floats of one psi set
+    const int nseg = (K + CKPT - 1) / CKPT;
+    CK(c->buf[B_FIDX].ensure((size_t)steps * 4));
+    CK(cudaMemcpyAsync(c->buf[B_FIDX].p, fidx.data(), (size_t)steps * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(c->buf[B_CXYZ].ensure((size_t)nb * c->natoms * 12));
+    CK(c->buf[B_CBOX].ensure((size_t)nb * 12));
+    CK(c->buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
+    CK(c->buf[B_A].ensure((size_t)nb * mstride * 4));
+    CK(c->buf[B_Z].ensure((size_t)nb * mstride * 4));
+    CK(c->buf[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
+    CK(c->buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
+    CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
+    CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
+    CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
+    CK(c->buf[B_PSI].ensure(psz * 4));
+    CK(c->buf[B_LAM].ensure(psz * 4));
+    CK(c->buf[B_PA].ensure(psz * 4));
+    CK(c->buf[B_PB].ensure(psz * 4));
+    CK(c->buf[B_SEG].ensure(psz * (CKPT + 1) * 4));
+    CK(c->buf[B_CKPT].ensure(psz * nseg * 4));
+    CK(c->buf[B_R].ensure((size_t)S * mstride * 4));
+    CK(c->buf[B_T].ensure((size_t)S * mstride * 4));
+    CK(c->buf[B_TCF].ensure((size_t)steps * 48));
+    CK(c->buf[B_GRAD].ensure(CIR_NTHETA * 8));
+    CK(cudaMemsetAsync(c->buf[B_STATUS].p, 0, (size_t)nb * 4, c->stream));
+    CK(cudaMemsetAsync(c->buf[B_GRAD].p, 0, CIR_NTHETA * 8, c->stream));
+    float *A = c->buf[B_A].as<float>(), *W = c->buf[B_W].as<float>(), *M = c->buf[B_M].as<float>();
+    float *CT = c->buf[B_CT].as<float>(), *CB = c->buf[B_CBOX].as<float>();
+    float *psi = c->buf[B_PSI].as<float>(), *lam = c->buf[B_LAM].as<float>();
+    float *PA = c->buf[B_PA].as<float>(), *PB = c->buf[B_PB].as<float>();
+    float *seg = c->buf[B_SEG].as<float>(), *ckpt = c->buf[B_CKPT].as<float>();
+    float *R = c->buf[B_R].as<float>(), *T = c->buf[B_T].as<float>();
+    double *tcf = c->buf[B_TCF].as<double>(), *dgrad = c->buf[B_GRAD].as<double>();
+    int launches = 0;
+    // frames, Hamiltonians and eigendecompositions of every step (origin-major: b = s*K + k)
+    Group g = ctx_group(c);
+    k_gather_frames<<<dim3(8, nb), 256, 0, c->stream>>>(static_cast<const float *>(dxyz), static_cast<const float *>(dbox),
+                                                        c->buf[B_FIDX].as<int>(), g.natoms, S, K, K, 0,
+                                                        c->buf[B_CXYZ].as<float>(), CB);
+    CK(cudaGetLastError());
+    launches++;
+    BuildArgs ba = build_args(c, g);
+    ba.xyz = c->buf[B_CXYZ].as<float>();
+    ba.box = CB;
+    ba.ct = CT;
+    ba.H = A;
+    ba.ldh = ld;
+    ba.dip = M;
+    ba.pol = M + 3 * ld;
+    ba.ldv = ld;
+    ba.dip_fstride = 9LL * ld;
+    ba.pol_fstride = 9LL * ld;
+    CK(cir_launch_build(ba, nb, c->stream, &launches));
+    EighArgs e;
+    memset(&e, 0, sizeof e);
+    e.A = A;
+    e.W = W;
+    e.Z = c->buf[B_Z].as<float>();
+    e.DC = c->buf[B_DC].as<float>();
+    e.DE = c->buf[B_DE].as<float>();
+    e.mstride = mstride;
+    e.wstride = ld;
+    e.n = n;
+    e.ld = ld;
+    e.status = c->buf[B_STATUS].as<int>();
+    e.nchrom_mol = p.nchrom_mol;
+    e.precision = CIR_PREC_FP32;
+    e.err = c->buf[B_ERR].as<int>();
+    CK(cir_launch_eigh(e, nb, c->stream, &launches));
+    // forward: psi(0) = m(0); psi(k) = U_k psi(k-1); correlation terms per step; checkpoints
+    const long long sV = (long long)K * mstride, sWk = (long long)K * ld, sM = (long long)K * 9 * ld;
+    CK(cir_adj_psi_init(M, sM, ld, n, S, psi, c->stream));
+    launches++;
+    for (int k = 0; k < K; k++) {
+        if (k > 0 && (rc = psi_propagate(c, S, n, ld, A + (size_t)k * mstride, sV, W + (size_t)k * ld, sWk, p.dt, psi, PA,
+                                         launches)))
+            return rc;
+        CK(cir_adj_tcf(psi, M + (size_t)k * 9 * ld, sM, ld, n, S, tcf + (size_t)k * 6, (long long)K * 6, c->stream));
+        launches++;
+        if (k == 0 || (k + 1) % CKPT == 0) {
+            const int slot = k == 0 ? 0 : (k + 1) / CKPT;
+            if (slot < nseg) CK(cudaMemcpyAsync(ckpt + psz * slot, psi, psz * 4, cudaMemcpyDeviceToDevice, c->stream));
+        }
+    }
+    // loss: lineshapes of the damped, origin-averaged IR and VV sums against the targets
+    std::vector<double> htcf((size_t)steps * 6);
+    std::vector<int> hst(nb);
+    CK(cudaMemcpyAsync(htcf.data(), tcf, (size_t)steps * 48, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hst.data(), c->buf[B_STATUS].p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < nb; i++)
+        if (hst[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached");
+    std::vector<double> dcy(K), X[2];
+    for (int q = 0; q < 2; q++) X[q].assign((size_t)2 * K, 0.0);
+    for (int k = 0; k < K; k++) {
+        dcy[k] = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
+        for (int s = 0; s < S; s++)
+            for (int q = 0; q < 2; q++) {           // IR (terms 0, 1) and VV (terms 2, 3)
+                X[q][2 * k] += htcf[((size_t)s * K + k) * 6 + 2 * q] * dcy[k];
+                X[q][2 * k + 1] += htcf[((size_t)s * K + k) * 6 + 2 * q + 1] * dcy[k];
+            }
+    }
+    const int nfft = p.ntcfpoints + p.nzeros;
+    const float *tg[2] = {target_ir, target_vv};
+    double L = 0.0;
+    std::vector<double> gre[2], gim[2];
+    for (int q = 0; q < 2; q++) {
+        std::vector<double> y;
+        if ((rc = c2r_dev(c, X[q].data(), y))) return rc;
+        gre[q].assign(K, 0.0);
+        gim[q].assign(K, 0.0);
+        // dL/dX_k = sum over rows of dL/dy_i dy_i/dX_k; y_i = Re X_0 + 2 sum_k Re(X_k e^{2 pi i ik/n})
+        for (size_t r = 0; r < rows.size(); r++) {
+            const int i = rows[r];
+            const double ls = (float)y[i] / norm;      // the printed value, as lineshape_rows makes it
+            const double d = ls - tg[q][r];
+            L += d * d;
+            const double dy = 2.0 * d / norm;
+            gre[q][0] += dy;
+            for (int k = 1; k < K; k++) {
+                const double ang = 2.0 * CIR_PI * (double)((long long)i * k % nfft) / nfft;
+                gre[q][k] += 2.0 * dy * cos(ang);
+                gim[q][k] -= 2.0 * dy * sin(ang);
+            }
+        }
+        for (int k = 0; k < K; k++) {              // through the damping and 1/nsamples
+            gre[q][k] *= dcy[k];
+            gim[q][k] *= dcy[k];
+        }
+    }
+    // backward, one segment of CKPT steps at a time, last segment first
+    const float tau = (float)(p.dt / CIR_HBAR);
+    DthetaArgs dt{};
+    dt.sct = (long long)K * CT_NROW * ld;
+    dt.sbox = 3LL * K;
+    dt.ldg = ld;
+    dt.sG = mstride;
+    dt.maps = c->maps;
+    dt.n = n;
+    dt.ld = ld;
+    dt.nchrom_mol = p.nchrom_mol;
+    dt.ispecies = p.ispecies;
+    dt.out = dgrad;
+    for (int j = nseg - 1; j >= 0; j--) {
+        const int c0 = j * CKPT, c1 = std::min(K, c0 + CKPT);
+        const int base = c0 == 0 ? 0 : c0 - 1;        // seg slot q holds psi(base + q)
+        CK(cudaMemcpyAsync(seg, ckpt + psz * j, psz * 4, cudaMemcpyDeviceToDevice, c->stream));
+        for (int k = base + 1; k < c1; k++) {
+            float *dst = seg + psz * (k - base);
+            CK(cudaMemcpyAsync(dst, seg + psz * (k - 1 - base), psz * 4, cudaMemcpyDeviceToDevice, c->stream));
+            if ((rc = psi_propagate(c, S, n, ld, A + (size_t)k * mstride, sV, W + (size_t)k * ld, sWk, p.dt, dst, PA,
+                                    launches)))
+                return rc;
+        }
+        for (int k = c1 - 1; k >= c0; k--) {
+            // lambda(k) = w(k) + U_{k+1} lambda(k+1)
+            if (k < K - 1 && (rc = psi_propagate(c, S, n, ld, A + (size_t)(k + 1) * mstride, sV, W + (size_t)(k + 1) * ld,
+                                                 sWk, p.dt, lam, PA, launches)))
+                return rc;
+            CK(cir_adj_lambda_src(lam, M + (size_t)k * 9 * ld, sM, ld, n, S, (float)gre[0][k], (float)gim[0][k],
+                                  (float)gre[1][k], (float)gim[1][k], k == K - 1, c->stream));
+            launches++;
+            const float *Vk = A + (size_t)k * mstride;
+            if (k >= 1) {
+                // a = V^T lambda(k), b = V^T psi(k-1); R; G = V R V^T (into R)
+                GemmArgs ga{};
+                ga.A = Vk; ga.lda = ld; ga.sA = sV; ga.a_colmajor = false;
+                ga.B = lam; ga.ldb = CIR_PSI_LD; ga.sB = (long long)n * CIR_PSI_LD;
+                ga.C = PA; ga.ldc = CIR_PSI_LD; ga.sC = (long long)n * CIR_PSI_LD;
+                ga.M = n; ga.N = CIR_PSI_LD; ga.K = n;
+                GemmArgs gb = ga;
+                gb.B = seg + psz * (k - 1 - base);
+                gb.C = PB;
+                CK(cir_launch_gemm(ga, S, c->stream, &launches));
+                CK(cir_launch_gemm(gb, S, c->stream, &launches));
+                CK(cir_adj_build_R(PA, PB, W + (size_t)k * ld, sWk, n, S, tau, R, ld, mstride, c->stream));
+                launches++;
+                GemmArgs gt{};
+                gt.A = Vk; gt.lda = ld; gt.sA = sV; gt.a_colmajor = true;     // V
+                gt.B = R; gt.ldb = ld; gt.sB = mstride;                        // R row-major
+                gt.C = T; gt.ldc = ld; gt.sC = mstride;
+                gt.M = gt.N = gt.K = n;
+                GemmArgs gg = gt;
+                gg.A = T; gg.a_colmajor = false; gg.sA = mstride;              // T row-major
+                gg.B = Vk; gg.sB = sV;                                         // B(k, j) = V[j][k]
+                gg.C = R;
+                CK(cir_launch_gemm(gt, S, c->stream, &launches));
+                CK(cir_launch_gemm(gg, S, c->stream, &launches));
+            }
+            dt.ct = CT + (size_t)k * CT_NROW * ld;
+            dt.box = CB + 3 * (size_t)k;
+            dt.G = k >= 1 ? R : nullptr;
+            dt.psi = seg + psz * (k - base);
+            dt.lam0 = k == 0 ? lam : nullptr;
+            dt.gir_r = (float)gre[0][k];
+            dt.gir_i = (float)gim[0][k];
+            dt.gvv_r = (float)gre[1][k];
+            dt.gvv_i = (float)gim[1][k];
+            CK(cir_adj_dtheta(dt, S, c->stream));
+            launches++;
+        }
+    }
+    CK(cudaMemcpyAsync(grad, dgrad, CIR_NTHETA * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    count_launch(c, launches);
+    *loss = L;
     return CIR_OK;
 }

@@ -137,4 +137,31 @@ cudaError_t cir_launch_c2r(const double *X, int nx, int n, double *work0, double
 // F = I for nprop complex matrices
 cudaError_t cir_launch_identity(float *F, int n, int ldf, long long sF, int batch, cudaStream_t s, int *launches);
 
+
+// ---- differentiation form (k_adjoint.cu) ----
+constexpr int CIR_PSI_LD = 18;   // psi / lambda: n x 9 complex, row-major (re, im) pairs
+struct DthetaArgs {
+    const float *ct;      // chromophore table of the step's frame of origin 0; origin s at + s*sct
+    long long sct;
+    const float *box;     // box of that frame; origin s at + s*sbox
+    long long sbox;
+    const float *G;       // dL/dH of the step (row-major, ldg; origin s at + s*sG), or null at step 0
+    int ldg;
+    long long sG;
+    const float *psi;     // psi(k), n x 18 per origin
+    const float *lam0;    // lambda(0) at step 0, else null
+    float gir_r, gir_i, gvv_r, gvv_i;   // dL/dTCF of the step (IR, VV)
+    CirMaps maps;
+    int n, ld, nchrom_mol, ispecies;
+    double *out;          // [13] accumulated
+};
+cudaError_t cir_adj_psi_init(const float *M, long long sM, int ld, int n, int S, float *psi, cudaStream_t s);
+cudaError_t cir_adj_tcf(const float *psi, const float *M, long long sM, int ld, int n, int S, double *out, long long sout,
+                        cudaStream_t s);
+cudaError_t cir_adj_lambda_src(float *lam, const float *M, long long sM, int ld, int n, int S, float gir_r, float gir_i,
+                               float gvv_r, float gvv_i, int zero, cudaStream_t s);
+cudaError_t cir_adj_build_R(const float *a, const float *b, const float *W, long long sW, int n, int S, float tau, float *R,
+                            int ldr, long long sR, cudaStream_t s);
+cudaError_t cir_adj_dtheta(const DthetaArgs &d, int S, cudaStream_t s);
+
 #endif

@@ -229,6 +229,25 @@ int cir_lineshape(cir_ctx *c, const double *tcf, float *omega, float *intensity,
 int cir_run(cir_ctx *c, int nframes, const float *xyz, const float *box,
             const int *frame_of_step, cir_result *r);
 
+/* Differentiation form.  The 13 map and coupling coefficients of calcIR.cu:1207-1242 in the
+ * order w0 w1 w2 (frequency map), x0 x1 (position matrix element, which also scales the
+ * polarisabilities), p0 p1 (momentum), mup0 mup1 mup2 (dipole derivative), wi0 wi1 wi2
+ * (intramolecular coupling).  cir_set_coeffs replaces the context's coefficients for every
+ * later call (targets, finite differences, fits). */
+#define CIR_NTHETA 13
+int cir_get_coeffs(cir_ctx *c, float *theta);
+int cir_set_coeffs(cir_ctx *c, const float *theta);
+
+/* The backward entry: L = sum over the printed lineshape rows of (IR - target_ir)^2 +
+ * (VV - target_vv)^2 for the job cir_run would compute on these frames, and dL/dtheta
+ * (grad [CIR_NTHETA], double).  The adjoint runs through the propagation (psi_c = F m_c(0),
+ * checkpointed every 16 steps and recomputed in the backward pass) and the eigendecompositions
+ * (the Daleckii-Krein divided difference of exp(i L dt/hbar), finite for equal eigenvalues),
+ * then through the maps.  FP32 with FP64 sums; nls must equal the lineshape's row count.
+ * Extends cir_run (calcIR.cu:360-839); the reference has no gradient. */
+int cir_loss_grad(cir_ctx *c, int nframes, const float *xyz, const float *box, const int *frame_of_step,
+                  const float *target_ir, const float *target_vv, int nls, double *loss, double *grad);
+
 /* One trajectory of a multi-trajectory job. */
 typedef struct cir_traj_in {
     int          natoms;          /* its own system size (a multiple of natom_mol)           */
