@@ -225,6 +225,77 @@ def run_batching(args):
     print(json.dumps(line), flush=True)
 
 
+DIFF_JOB = dict(model="tip4p2005", species="H2O", ntcfpoints=200, nsamples=4, sampleEvery=2.0, dt=0.010, t1=0.260,
+                avef=3415.0, omegaStart=2000, omegaStop=5000, omegaStep=1, nzeros=25600, map=0)
+
+
+def run_differentiation(args):
+    """The differentiation configuration: 256 TIP4P/2005 molecules (512 chromophores), 4 time
+    origins x 200 points; the loss is the IR + VV lineshape mismatch against targets made by
+    the same code with the map coefficients perturbed by seeded +-2% noise.  One bench step is
+    one loss + gradient evaluation (cir_loss_grad: forward, psi checkpoints every 16 steps,
+    adjoint backward).  The gradient is checked against GPU central differences (relative
+    step 1e-4) on the three coefficients the loss is most sensitive to."""
+    import torch
+    torch.cuda.set_device(0)
+    from calcir_gb300 import build
+    build.build()
+    import calcir_gb300 as cg
+    q = cg.default_params(**DIFF_JOB)
+    fos = cg.frame_table(q, 0.010)
+    xyz, box = cg.synth_trajectory(256, int(fos.max()) + 1, seed=args.seed)
+    stream = torch.cuda.current_stream()
+    with cg.Engine(q, xyz.shape[1]) as eng:
+        eng.set_stream(stream.cuda_stream)
+        th0 = eng.get_coeffs().astype(np.float64)
+        tht = th0 * (1 + 0.02 * np.random.default_rng(args.seed).uniform(-1, 1, 13))
+        eng.set_coeffs(tht.astype(np.float32))
+        ref = eng.run(xyz, box, fos)
+        targets = (ref["ls_ir"].astype(np.float32), ref["ls_vv"].astype(np.float32))
+        eng.set_coeffs(th0.astype(np.float32))
+        warm = max(3, args.warmup)
+        for _ in range(warm):
+            eng.loss_grad(xyz, box, fos, *targets)
+        eng.reset_stats()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(gpu_identifier())
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            L, g = eng.loss_grad(xyz, box, fos, *targets)
+        torch.cuda.synchronize()
+        sec = (time.perf_counter() - t0) / args.steps
+        clk = sampler.stop()
+        st = eng.stats()
+        sens = np.abs(g * th0)
+        checks = []
+        for qi in np.argsort(-sens)[:3]:
+            h = 1e-4 * abs(th0[qi])
+            lv = []
+            for sgn in (1, -1):
+                t = th0.copy()
+                t[qi] += sgn * h
+                eng.set_coeffs(t.astype(np.float32))
+                lv.append(eng.loss_grad(xyz, box, fos, *targets)[0])
+            step = float(np.float32(th0[qi] + h)) - float(np.float32(th0[qi] - h))
+            fd = (lv[0] - lv[1]) / step
+            checks.append({"coefficient": ["w0", "w1", "w2", "x0", "x1", "p0", "p1", "mup0", "mup1", "mup2", "wi0",
+                                           "wi1", "wi2"][qi], "adjoint": float(g[qi]), "central_difference": fd,
+                           "rel_diff": abs(fd - g[qi]) / abs(g[qi])})
+        eng.set_coeffs(th0.astype(np.float32))
+    nsteps = len(fos)
+    line = {
+        "metric": "frame-steps/s of loss + adjoint gradient, differentiation: 256 H2O, 4 origins x 200 points",
+        "value": nsteps / sec, "unit": "frame-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": warm,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "256 TIP4P/2005 molecules (512 chromophores), 4 origins 2 ps apart x 200 points; "
+                               "targets from map coefficients perturbed by seeded +-2% noise; psi checkpoints every "
+                               "16 steps", "loss": L},
+        "gradient_checks": checks, "gpu_launches": int(st["kernel_launches"]), "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -237,7 +308,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=8, help="frame-steps per CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="full", choices=["full", "batching"],
+    ap.add_argument("--workload", default="full", choices=["full", "batching", "differentiation"],
                     help="full: the 512 H2O job (the headline); batching: uneven boxes of 128/216/343/512 "
                          "molecules, --batching-traj trajectories of each size, in one cir_run_multi job")
     ap.add_argument("--batching-traj", type=int, default=32)
@@ -246,6 +317,8 @@ def main():
         return run_reference_arm(args)
     if args.workload == "batching":
         return run_batching(args)
+    if args.workload == "differentiation":
+        return run_differentiation(args)
 
     import torch
     rank, world, local = dist_env()

@@ -77,7 +77,7 @@ def test_autograd_wrapper_and_gpu_central_difference(lib):
         eng.set_coeffs(th0.astype(np.float32))
         L, g = eng.loss_grad(xyz, box, fos, targets[0], targets[1])
         np.testing.assert_allclose(theta.grad.numpy(), g, rtol=1e-12)
-        assert float(loss) == pytest.approx(L, rel=1e-12)
+        assert float(loss.detach()) == pytest.approx(L, rel=1e-12)
         q = int(np.argmax(np.abs(g * th0)))
         h = 1e-4 * abs(th0[q])
         vals = []
