@@ -378,7 +378,7 @@ static int tuned_tile(cir_ctx *c, const GemmArgs &g, int batch) {
 // Must run outside stream capture.
 static int autotune_gemm(cir_ctx *c, const GemmArgs &g, int batch) {
     if (!c->p.autotune || c->gemm_tile.count(gemm_shape(g, batch))) return CIR_OK;
-    const size_t a_el = (size_t)(g.a_colmajor ? g.K : g.M) * g.lda, b_el = (size_t)g.K * g.ldb,
+    const size_t a_el = (size_t)(g.a_colmajor ? g.K : g.M) * g.lda, b_el = (size_t)(g.b_kmajor ? g.N : g.K) * g.ldb,
                  c_el = (size_t)g.M * g.ldc, w_el = g.epilogue == 1 ? (size_t)g.M : 0;
     const size_t tot = (a_el + b_el + c_el + w_el + 16) * batch * sizeof(float);
     CK(c->buf[B_TUNE].ensure(tot));

@@ -87,6 +87,10 @@ size_t cir_eigh_rot_bytes(int n);
 size_t cir_eigh_de_bytes(int ld);
 size_t cir_dc_bytes(int n, int ld);
 cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
+// V = Q_H Q into a.A by blocked compact-WY application of the tridiagonalisation's
+// reflectors (in a.A) to Q; Q is overwritten, P is scratch (a.mstride floats per matrix),
+// a.Z holds the blocks' T^T V^T.
+cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, int nmat, cudaStream_t s, int *launches);
 int cir_eigh_max_n();
 
 // batched SIMT FP32 GEMM, C = A * B (row-major B, C); A row- or column-major.
@@ -98,7 +102,11 @@ struct GemmArgs {
     int lda, ldb, ldc;
     long long sA, sB, sC;  // batch strides (elements)
     bool a_colmajor;
-    int epilogue;          // 0 none, 1 phase rotation
+    bool b_kmajor;         // B element (k, n) at B[n*ldb + k] instead of B[k*ldb + n]
+    int epilogue;          // 0 none, 1 phase rotation, 2 C = D - A B
+    const float *D;        // epilogue 2 (may equal C)
+    int ldd;
+    long long sD;
     const float *w;        // [batch][wstride] for epilogue 1
     int wstride;
     float dt_over_hbar;

@@ -22,8 +22,9 @@
 //     row-major, and the eigenvalues ascending.
 //   * k_dc_gemm: Q_new = diag(Q1, Q2) U for every merge, as two products of the diagonal
 //     blocks with the matching rows of U (64 x 64 tiles, FP32).
-// The eigenvectors of H are then V = Q_H Q_T (Q_H formed by k_eigh_formq), one batched GEMM:
-// FP32 in the plain form, the tensor-core GEMM (a.precision) in the mixed forms.
+// The eigenvectors of H are then V = Q_H Q_T, the reflectors of the tridiagonalisation
+// applied to Q_T in compact WY blocks (k_backtransform.cu): FP32 GEMMs in the plain form,
+// the tensor-core GEMM (a.precision) in the mixed forms.
 #include "cir_device.cuh"
 #include <float.h>
 
@@ -503,8 +504,8 @@ int dc_depth(int n) {
 size_t cir_dc_bytes(int n, int ld) { return sizeof(float) * 3 * (size_t)n * ld; }
 
 // Stage 2 of the divide-and-conquer eigensolver: everything after the tridiagonalisation
-// (DE holds d, e, tau) and the formation of Q_H in a.Z.  a.DC: 3 buffers of a.mstride
-// floats per matrix (Q_T ping, pong, U), laid out [buffer][matrix].
+// (DE holds d, e, tau; A the reflectors).  a.DC: 3 buffers of a.mstride floats per matrix
+// (Q_T ping, pong, U), laid out [buffer][matrix]; a.Z is scratch of the back-transform.
 cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *launches) {
     const int n = a.n, ld = a.ld;
     const int D = dc_depth(n);
@@ -562,22 +563,12 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
         if (e != cudaSuccess) return e;
         cur = other;
     }
-    // V = Q_H Q_T: in the row-major view of the column-major buffers, V^T = Q_T^T Q_H^T
-    GemmArgs g{};
-    g.A = buf[cur];
-    g.B = a.Z;
-    g.C = a.A;
-    g.M = g.N = g.K = n;
-    g.lda = g.ldb = g.ldc = ld;
-    g.sA = g.sB = g.sC = a.mstride;
-    g.a_colmajor = false;
-    g.epilogue = 0;
-    g.err = a.err;
-    e = a.precision == CIR_PREC_FP32 ? cir_launch_gemm(g, nmat, s, nullptr)
-                                     : cir_launch_tc_gemm(g, nmat, a.precision, s, nullptr);
+    // V = Q_H Q_T into a.A: the reflectors applied to Q_T (buf[cur]) in compact WY blocks,
+    // with the free ping-pong buffer as scratch
+    e = cir_launch_backtransform(a, buf[cur], buf[cur ^ 1], nmat, s, &nl);
     if (e != cudaSuccess) return e;
     k_dc_finish<<<nmat, 256, 0, s>>>(a);
-    nl += 2;
+    nl += 1;
     if (launches) *launches += nl;
     return cudaGetLastError();
 }

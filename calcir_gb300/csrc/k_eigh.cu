@@ -10,7 +10,10 @@
 //     orders: the rank-2 update of step k-1 and the matrix-vector product of step k share
 //     one read/write pass over the trailing block.
 //  2. Q is formed explicitly in Z by backward accumulation of the reflectors in compact WY
-//     blocks, each warp holding its rows of the block's reflectors in registers.
+//     blocks, each warp holding its rows of the block's reflectors in registers.  (The
+//     divide-and-conquer path, a.DC set, skips phases 2-4: it solves the tridiagonal
+//     problem in k_dc.cu and applies the reflectors to its eigenvectors afterwards,
+//     k_backtransform.cu.)
 //  3. Implicit symmetric QR on T with the Wilkinson shift (Golub & Van Loan, Alg. 8.3.2).
 //     Lane 0 of warp 0 chases the bulges of a group of EIG_KS sweeps (the bulge state is
 //     carried in registers) while the other warps apply the previous group to the rows
@@ -1208,12 +1211,14 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     else e = launch_tq<256, 2048, 2, true>(a, nmat, s);
     if (e != cudaSuccess) return e;
     if (a.tq_done && (e = cudaEventRecord(a.tq_done, s)) != cudaSuccess) return e;
+    if (launches) *launches += 1;
+    // divide and conquer: the reflectors are applied to the tridiagonal eigenvectors at the end
+    if (a.DC) return cir_launch_dc(a, nmat, s, launches);
     if (a.n <= 512) e = launch_formq<256, 512, 16, 8, 2>(a, nmat, s);
     else if (a.n <= 1024) e = launch_formq<256, 1024, 16, 8, 2>(a, nmat, s);
     else e = launch_formq<256, 2048, 8, 4, 2>(a, nmat, s);
     if (e != cudaSuccess) return e;
-    if (launches) *launches += 2;
-    if (a.DC) return cir_launch_dc(a, nmat, s, launches);
+    if (launches) *launches += 1;
     e = launch_qr(a, nmat, s);
     if (launches) *launches += 1;
     return e;

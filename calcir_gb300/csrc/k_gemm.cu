@@ -63,9 +63,22 @@ __device__ __forceinline__ void store_a(float (*As)[T::BM], const float (&ra)[4]
     }
 }
 
-template <class T>
+template <class T, bool BKC>
 __device__ __forceinline__ void load_b(const GemmArgs &g, const float *B, int k0, int n0, float (&rb)[4]) {
     const int t = threadIdx.x;
+    if (BKC) {    // element (k, j) at B[j*ldb + k]; thread loads 4 consecutive k of one j
+        const int j = t / (T::BK / 4), kk = (t % (T::BK / 4)) * 4;
+        const int gj = n0 + j, gk = k0 + kk;
+        const float *p = B + (size_t)gj * g.ldb + gk;
+        if (gj < g.N && gk + 3 < g.K && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+            const float4 v = *reinterpret_cast<const float4 *>(p);
+            rb[0] = v.x; rb[1] = v.y; rb[2] = v.z; rb[3] = v.w;
+        } else {
+            #pragma unroll
+            for (int q = 0; q < 4; q++) rb[q] = (gj < g.N && gk + q < g.K) ? p[q] : 0.f;
+        }
+        return;
+    }
     const int kk = t / (T::BN / 4), j = (t % (T::BN / 4)) * 4;
     const int gk = k0 + kk, gj = n0 + j;
     const float *p = B + (size_t)gk * g.ldb + gj;
@@ -78,7 +91,20 @@ __device__ __forceinline__ void load_b(const GemmArgs &g, const float *B, int k0
     }
 }
 
-template <class T, bool ACOL>
+template <class T, bool BKC>
+__device__ __forceinline__ void store_b(float (*Bs)[T::BN], const float (&rb)[4]) {
+    const int t = threadIdx.x;
+    if (BKC) {
+        const int j = t / (T::BK / 4), kk = (t % (T::BK / 4)) * 4;
+        #pragma unroll
+        for (int q = 0; q < 4; q++) Bs[kk + q][j] = rb[q];
+    } else {
+        const int kk = t / (T::BN / 4), j = (t % (T::BN / 4)) * 4;
+        *reinterpret_cast<float4 *>(&Bs[kk][j]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+    }
+}
+
+template <class T, bool ACOL, bool BKC>
 __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
     constexpr int BM = T::BM, BN = T::BN, BK = T::BK, TM = T::TM, TN = T::TN;
     __shared__ __align__(16) float As[2][BK][BM];
@@ -98,19 +124,16 @@ __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
 
     float ra[4], rb[4];
     load_a<T, ACOL>(g, A, m0, 0, ra);
-    load_b<T>(g, B, 0, n0, rb);
+    load_b<T, BKC>(g, B, 0, n0, rb);
     store_a<T, ACOL>(As[0], ra);
-    {
-        const int kk = threadIdx.x / (BN / 4), j = (threadIdx.x % (BN / 4)) * 4;
-        *reinterpret_cast<float4 *>(&Bs[0][kk][j]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
-    }
+    store_b<T, BKC>(Bs[0], rb);
     __syncthreads();
     int buf = 0;
     for (int k0 = 0; k0 < g.K; k0 += BK) {
         const bool more = k0 + BK < g.K;
         if (more) {
             load_a<T, ACOL>(g, A, m0, k0 + BK, ra);
-            load_b<T>(g, B, k0 + BK, n0, rb);
+            load_b<T, BKC>(g, B, k0 + BK, n0, rb);
         }
         #pragma unroll
         for (int kk = 0; kk < BK; kk++) {
@@ -132,8 +155,7 @@ __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
         }
         if (more) {
             store_a<T, ACOL>(As[buf ^ 1], ra);
-            const int kk = threadIdx.x / (BN / 4), j = (threadIdx.x % (BN / 4)) * 4;
-            *reinterpret_cast<float4 *>(&Bs[buf ^ 1][kk][j]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+            store_b<T, BKC>(Bs[buf ^ 1], rb);
         }
         __syncthreads();
         buf ^= 1;
@@ -160,6 +182,11 @@ __global__ void __launch_bounds__(GT) k_sgemm(GemmArgs g) {
                     v[q + 1] = sph * re + cph * im;
                 }
             }
+            if (g.epilogue == 2) {   // C = D - A B
+                const float *d = g.D + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                #pragma unroll
+                for (int q = 0; q < 4; q++) v[q] = (c + q < g.N ? d[q] : 0.f) - v[q];
+            }
             float *p = C + (size_t)r * g.ldc + c;
             if (c + 3 < g.N && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
                 *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
@@ -181,15 +208,17 @@ __global__ void k_identity(float *F, int n, int ldf, long long sF) {
 template <class T>
 cudaError_t launch_sgemm(const GemmArgs &g, int batch, cudaStream_t s) {
     dim3 grid((g.N + T::BN - 1) / T::BN, (g.M + T::BM - 1) / T::BM, batch);
-    if (g.a_colmajor) k_sgemm<T, true><<<grid, GT, 0, s>>>(g);
-    else k_sgemm<T, false><<<grid, GT, 0, s>>>(g);
+    if (g.a_colmajor && g.b_kmajor) return cudaErrorInvalidValue;
+    if (g.a_colmajor) k_sgemm<T, true, false><<<grid, GT, 0, s>>>(g);
+    else if (g.b_kmajor) k_sgemm<T, false, true><<<grid, GT, 0, s>>>(g);
+    else k_sgemm<T, false, false><<<grid, GT, 0, s>>>(g);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *launches, int tile) {
-    if (g.epilogue == 1 && (g.N & 1)) return cudaErrorInvalidValue;
+    if ((g.epilogue == 1 && (g.N & 1)) || (g.epilogue == 2 && !g.D)) return cudaErrorInvalidValue;
     if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     const cudaError_t e = tile == CIR_GEMM_TILE_64 ? launch_sgemm<TileS>(g, batch, s) : launch_sgemm<TileL>(g, batch, s);
     if (launches) *launches += 1;

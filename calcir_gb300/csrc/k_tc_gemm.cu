@@ -1,7 +1,8 @@
 // Tensor-core (tcgen05) GEMM for the propagation step of the mixed-precision form:
-// C[b] = A[b] * B[b] with FP32 accumulation in tensor memory, B row-major (N contiguous),
-// A row-major (K contiguous) or column-major (M contiguous), optional fused phase
-// rotation of (re, im) column pairs in the epilogue (see k_gemm.cu for the step).
+// C[b] = A[b] * B[b] with FP32 accumulation in tensor memory, B row-major (N contiguous) or
+// K-major, A row-major (K contiguous) or column-major (M contiguous), optional fused phase
+// rotation of (re, im) column pairs in the epilogue (see k_gemm.cu for the step) or
+// C = D - A B (the Householder back-transform of the eigensolver).
 //
 // One CTA computes a 128 x 128 tile with 128 threads:
 //   * all threads stage 32-deep K slices of A and B from global memory into shared
@@ -223,7 +224,7 @@ struct Slice {
     }
 };
 
-template <bool ACOL, int MODE>
+template <bool ACOL, bool BKC, int MODE>
 __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
     using C_ = Cfg<MODE>;
     constexpr int TB = tile_bytes<MODE>();
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
     constexpr uint32_t IDESC = make_idesc(C_::FMT);
 
     Slice<!ACOL> la;    // A: K contiguous unless column-major
-    Slice<false> lb;    // B: N contiguous
+    Slice<BKC> lb;      // B: N contiguous unless K-major
     const int KT = (g.K + TK - 1) / TK;
     bool ok = true;
     la.load(g.A + (size_t)bz * g.sA, g.lda, g.M, g.K, m0, 0);
@@ -320,6 +321,11 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
                 }
             }
             const int c = n0 + c0;
+            if (g.epilogue == 2) {   // C = D - A B
+                const float *d = g.D + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                #pragma unroll
+                for (int q = 0; q < 16; q++) v[q] = (c + q < g.N ? d[q] : 0.f) - v[q];
+            }
             float *p = C + (size_t)r * g.ldc + c;
             if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
                 #pragma unroll
@@ -342,14 +348,22 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
 template <int MODE>
 __host__ __device__ constexpr size_t smem_bytes() { return 4 * (size_t)Cfg<MODE>::PARTS * tile_bytes<MODE>() + 64; }
 
-template <bool ACOL, int MODE>
+template <bool ACOL, bool BKC, int MODE>
 cudaError_t launch(const GemmArgs &g, int batch, cudaStream_t s) {
     const size_t smem = smem_bytes<MODE>();
     dim3 grid((g.N + TN - 1) / TN, (g.M + TM - 1) / TM, batch);
-    cudaError_t e = cudaFuncSetAttribute(k_tc_gemm<ACOL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_tc_gemm<ACOL, BKC, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_tc_gemm<ACOL, MODE><<<grid, NTHREADS, smem, s>>>(g);
+    k_tc_gemm<ACOL, BKC, MODE><<<grid, NTHREADS, smem, s>>>(g);
     return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_mode(const GemmArgs &g, int batch, cudaStream_t s) {
+    if (g.a_colmajor && g.b_kmajor) return cudaErrorInvalidValue;
+    if (g.a_colmajor) return launch<true, false, MODE>(g, batch, s);
+    if (g.b_kmajor) return launch<false, true, MODE>(g, batch, s);
+    return launch<false, false, MODE>(g, batch, s);
 }
 
 }  // namespace
@@ -357,10 +371,11 @@ cudaError_t launch(const GemmArgs &g, int batch, cudaStream_t s) {
 size_t cir_tc_gemm_smem_bytes() { return smem_bytes<CIR_PREC_BF16X3>(); }
 
 cudaError_t cir_launch_tc_gemm(const GemmArgs &g, int batch, int precision, cudaStream_t s, int *launches) {
-    if (g.epilogue == 1 && (g.N & 1)) return cudaErrorInvalidValue;
+    if ((g.epilogue == 1 && (g.N & 1)) || (g.epilogue == 2 && !g.D)) return cudaErrorInvalidValue;
+    if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     cudaError_t e;
-    if (precision == CIR_PREC_TF32) e = g.a_colmajor ? launch<true, CIR_PREC_TF32>(g, batch, s) : launch<false, CIR_PREC_TF32>(g, batch, s);
-    else if (precision == CIR_PREC_BF16X3) e = g.a_colmajor ? launch<true, CIR_PREC_BF16X3>(g, batch, s) : launch<false, CIR_PREC_BF16X3>(g, batch, s);
+    if (precision == CIR_PREC_TF32) e = launch_mode<CIR_PREC_TF32>(g, batch, s);
+    else if (precision == CIR_PREC_BF16X3) e = launch_mode<CIR_PREC_BF16X3>(g, batch, s);
     else return cudaErrorInvalidValue;
     if (e != cudaSuccess) return e;
     if (launches) *launches += 1;
