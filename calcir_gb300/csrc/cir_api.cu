@@ -53,6 +53,7 @@ enum {
     B_TCF, B_HCNT, B_HIPR, B_HMIPR, B_OOR, B_SW, B_MU2, B_SWEEPS, B_ROT, B_PAD,
     B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR, B_DC, B_TUNE,
     B_PSI, B_LAM, B_PA, B_PB, B_SEG, B_CKPT, B_R, B_T, B_GRAD,   // differentiation form
+    B_VS, B_FS,                                    // split-BF16 propagation operands
     B_COUNT
 };
 
@@ -108,6 +109,7 @@ static void eigh_profile_report(const unsigned long long *dev, int nmat, cudaStr
     if (cudaMemcpyAsync(h.data(), dev, h.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) return;
     cudaStreamSynchronize(s);
     double tri = 0, fq = 0, qr = 0, srt = 0, chase = 0, apply = 0, nrot = 0, search = 0, sweeps = 0;
+    double tqp[6] = {0, 0, 0, 0, 0, 0};
     unsigned long long t0 = ~0ull, t1 = 0;
     for (int m = 0; m < nmat; m++) {
         const unsigned long long *r = h.data() + (size_t)m * S;
@@ -116,17 +118,23 @@ static void eigh_profile_report(const unsigned long long *dev, int nmat, cudaStr
         qr += (double)(r[5] - r[4]);
         srt += (double)(r[6] - r[5]);
         t0 = std::min(t0, r[0]);
-        t1 = std::max(t1, r[6]);
+        t1 = std::max(t1, r[1]);
         chase += (double)r[7];
         apply += (double)r[8];
         nrot += (double)r[9];
         search += (double)r[10];
         sweeps += (double)r[11];
+        for (int q = 0; q < 6; q++) tqp[q] += (double)r[12 + q];
     }
-    fprintf(stderr, "eigh profile: %d matrices, span %.3f ms; mean per block (ms): tridiag %.3f formQ %.3f qr %.3f "
+    fprintf(stderr, "eigh profile: %d matrices, tridiagonalisation span %.3f ms; mean per block (ms): tridiag %.3f formQ %.3f qr %.3f "
                     "(chase %.3f incl. block search %.3f, apply %.3f, %.0f rotations in %.0f sweeps) sort %.3f\n",
             nmat, (t1 - t0) * 1e-6, tri / nmat * 1e-6, fq / nmat * 1e-6, qr / nmat * 1e-6, chase / nmat * 1e-6,
             search / nmat * 1e-6, apply / nmat * 1e-6, nrot / nmat, sweeps / nmat, srt / nmat * 1e-6);
+    if (tqp[0] + tqp[2] > 0)
+        fprintf(stderr, "eigh profile: tridiagonalisation phases, mean per block (ms): column %.3f reflector %.3f "
+                        "symv %.3f panel dots %.3f w %.3f trailing update %.3f\n",
+                tqp[0] / nmat * 1e-6, tqp[1] / nmat * 1e-6, tqp[2] / nmat * 1e-6, tqp[3] / nmat * 1e-6,
+                tqp[4] / nmat * 1e-6, tqp[5] / nmat * 1e-6);
 }
 
 static int count_launch(cir_ctx *c, int k) {
@@ -600,10 +608,10 @@ __global__ void k_copy_m0(const float *m, long long sm_origin, int rows_ld, floa
 // Launch key of a captured step loop: every shape and pointer its launches depend on.
 static std::vector<long long> step_key(const Group &g, int St, int K, int k0, int kc, int precision, const void *A,
                                        const void *W, const void *M, const void *F, const void *G, const void *M0,
-                                       const void *tcf, int tile1, int tile2) {
+                                       const void *tcf, int tile1, int tile2, const void *VS, const void *FS) {
     return {g.n, g.ld, St, K, k0, kc, precision, (long long)(uintptr_t)A, (long long)(uintptr_t)W,
             (long long)(uintptr_t)M, (long long)(uintptr_t)F, (long long)(uintptr_t)G, (long long)(uintptr_t)M0,
-            (long long)(uintptr_t)tcf, tile1, tile2};
+            (long long)(uintptr_t)tcf, tile1, tile2, (long long)(uintptr_t)VS, (long long)(uintptr_t)FS};
 }
 
 // The frame-steps of one group: ntraj trajectories of one size, nsamples origins each.
@@ -643,8 +651,18 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
     CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
     CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
     CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
-    CK(c->buf[B_F].ensure((size_t)St * n * 2 * ld * 4));
-    CK(c->buf[B_G].ensure((size_t)St * n * 2 * ld * 4));
+    // the split-BF16 form propagates pre-split operands (k_tc_split.cu): per origin the
+    // step's V as Vc and Vr and the transposed F and G, each a hi/lo pair of order ldh
+    const bool split = p.precision == CIR_PREC_BF16X3;
+    const int ldh = (int)cir_split_ld(n);
+    const long long vs_el = (long long)n * ldh, fs_el = (long long)2 * n * ldh;   // elements per origin
+    if (split) {
+        CK(c->buf[B_VS].ensure((size_t)4 * St * vs_el * 2));
+        CK(c->buf[B_FS].ensure((size_t)4 * St * fs_el * 2));
+    } else {
+        CK(c->buf[B_F].ensure((size_t)St * n * 2 * ld * 4));
+        CK(c->buf[B_G].ensure((size_t)St * n * 2 * ld * 4));
+    }
     CK(c->buf[B_M0].ensure((size_t)St * 9 * ld * 4));
     CK(c->buf[B_TCF].ensure((size_t)steps * 6 * 8));
     CK(c->buf[B_HCNT].ensure((size_t)T * nomega * 8));
@@ -665,6 +683,10 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
 
     float *A = c->buf[B_A].as<float>(), *W = c->buf[B_W].as<float>(), *M = c->buf[B_M].as<float>();
     float *F = c->buf[B_F].as<float>(), *G = c->buf[B_G].as<float>(), *M0 = c->buf[B_M0].as<float>();
+    __nv_bfloat16 *vs = split ? c->buf[B_VS].as<__nv_bfloat16>() : nullptr;
+    __nv_bfloat16 *fs = split ? c->buf[B_FS].as<__nv_bfloat16>() : nullptr;
+    const SplitMat Vc{vs, vs + St * vs_el}, Vr{vs + 2 * St * vs_el, vs + 3 * St * vs_el};
+    const SplitMat Ft{fs, fs + St * fs_el}, Gt{fs + 2 * St * fs_el, fs + 3 * St * fs_el};
     double *tcf = c->buf[B_TCF].as<double>();
     int launches = 0;
     cudaEvent_t *ev = c->ev;
@@ -747,7 +769,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                                        p.omegaStep, p.t1, p.avef, c->stream, &launches));
             }
             // F = I and the t = 0 vectors (calcIR.cu:577-594)
-            CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, St, c->stream, &launches));
+            if (split) CK(cir_launch_identity_t(Ft, n, ldh, fs_el, St, c->stream, &launches));
+            else CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, St, c->stream, &launches));
             k_copy_m0<<<dim3(4, St), 256, 0, c->stream>>>(M, (long long)kc * 9 * ld, ld, M0);
             CK(cudaGetLastError());
             launches++;
@@ -757,7 +780,25 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         auto run_steps = [&](int &nl) -> int {
             for (int k = k0; k < k0 + kc; k++) {
                 const int kk = k - k0;
-                if (k > 0) {
+                if (k > 0 && split) {
+                    CK(cir_launch_split_v(A + (size_t)kk * mstride, ld, (long long)kc * mstride, n, Vc, Vr, ldh, vs_el,
+                                          St, c->stream, &nl));
+                    SplitGemmArgs s1{};
+                    s1.Ahi = Vc.hi; s1.Alo = Vc.lo; s1.lda = ldh; s1.sA = vs_el;       // V^T
+                    s1.Bhi = Ft.hi; s1.Blo = Ft.lo; s1.ldb = ldh; s1.sB = fs_el;       // F
+                    s1.Chi = Gt.hi; s1.Clo = Gt.lo; s1.ldc = ldh; s1.sC = fs_el;       // G, transposed
+                    s1.M = n; s1.N = 2 * n; s1.K = n;
+                    s1.epilogue = 1; s1.w = W + (size_t)kk * ld; s1.wstride = kc * ld;
+                    s1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
+                    s1.err = c->buf[B_ERR].as<int>();
+                    SplitGemmArgs s2 = s1;
+                    s2.Ahi = Vr.hi; s2.Alo = Vr.lo;                                    // V
+                    s2.Bhi = Gt.hi; s2.Blo = Gt.lo;
+                    s2.Chi = Ft.hi; s2.Clo = Ft.lo;                                    // F', transposed
+                    s2.epilogue = 0;
+                    CK(cir_launch_split_gemm(s1, St, c->stream, &nl));
+                    CK(cir_launch_split_gemm(s2, St, c->stream, &nl));
+                } else if (k > 0) {
                     int rc2 = propagate_dev(c, St, n, A + (size_t)kk * mstride, ld, (long long)kc * mstride,
                                             W + (size_t)kk * ld, kc * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);
                     if (rc2) return rc2;
@@ -775,12 +816,17 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                 t.n = n;
                 t.ldf = 2 * ld;
                 t.ldv = ld;
+                if (split) {
+                    t.Ft = Ft;
+                    t.sFt = fs_el;
+                    t.ldft = ldh;
+                }
                 CK(cir_launch_tcf(t, St, c->stream, &nl));
             }
             return CIR_OK;
         };
         if (p.cuda_graphs) {
-            const std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2);
+            const std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2, vs, fs);
             GraphEntry *ge = nullptr;
             for (auto &x : c->graphs)
                 if (x.key == key) ge = &x;

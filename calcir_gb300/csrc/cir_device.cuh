@@ -3,6 +3,7 @@
 #define CIR_DEVICE_CUH_
 
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include "cir_internal.h"
 
 // minImage (calcIR.cu:1459-1463): dx - L*round(dx/L), round half away from zero.
@@ -48,7 +49,7 @@ struct BuildArgs {
     CirMaps maps;
 };
 
-constexpr int CIR_EIG_PROF_SLOTS = 12;
+constexpr int CIR_EIG_PROF_SLOTS = 18;
 
 struct EighArgs {
     float *A;             // [nmat] matrices, column j of matrix m at A + m*mstride + j*ld
@@ -77,6 +78,8 @@ struct EighArgs {
     // optional [nmat][CIR_EIG_PROF_SLOTS]: %globaltimer at the start and end of the
     // tridiagonalisation, of forming Q, of the QR iteration and of the ordering (0-6), then the
     // chase and apply times (ns), rotations, the chase's block-search time (ns) and sweeps
+    // (7-11), then the blocked tridiagonalisation's time (ns) in its column fetch, reflector,
+    // symmetric matrix-vector product, panel dot products, w and trailing update (12-17)
     unsigned long long *phase_ns;
 };
 
@@ -119,6 +122,35 @@ cudaError_t cir_launch_gemm(const GemmArgs &g, int batch, cudaStream_t s, int *l
 cudaError_t cir_launch_tc_gemm(const GemmArgs &g, int batch, int precision, cudaStream_t s, int *launches);
 size_t cir_tc_gemm_smem_bytes();
 
+// ---- split-BF16 propagation on pre-split operands (k_tc_split.cu) ----
+// A matrix held as two BF16 matrices, hi = bf16(x) and lo = bf16(x - hi).
+struct SplitMat {
+    __nv_bfloat16 *hi, *lo;
+};
+// C = A B (hi*hi + hi*lo + lo*hi, FP32 accumulation) with K-major operands:
+// A(i, k) at A[i*lda + k], B(k, j) at B[j*ldb + k]; C(i, j) written as hi/lo at C[j*ldc + i].
+// lda, ldb and the batch strides are multiples of 8, the operand pointers 16-byte aligned.
+// epilogue 1: columns (2q, 2q+1) of row i rotated by exp(+i w[i] dt/hbar) before the split.
+struct SplitGemmArgs {
+    const __nv_bfloat16 *Ahi, *Alo, *Bhi, *Blo;
+    __nv_bfloat16 *Chi, *Clo;
+    int M, N, K;
+    int lda, ldb, ldc;
+    long long sA, sB, sC;
+    int epilogue;
+    const float *w;
+    int wstride;
+    float dt_over_hbar;
+    int *err;
+};
+size_t cir_split_ld(int n);   // leading dimension of the split operands (n rounded up to 8)
+cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches);
+// Vc = V (V[k][i] at A[i*ld + k]) and Vr = V^T, both as Vc[i*ldh + k]-style K-major pairs
+cudaError_t cir_launch_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh,
+                               long long sV, int batch, cudaStream_t s, int *launches);
+// Ft = I for the transposed complex F (real column c = 2q + {0: re, 1: im} at Ft[c*ldh ..])
+cudaError_t cir_launch_identity_t(SplitMat F, int n, int ldh, long long sF, int batch, cudaStream_t s, int *launches);
+
 // TCF terms: out[b][6] += (IR, VV, VH) for batch element b
 struct TcfArgs {
     const float *F;        // [batch] complex row-major, row stride ldf floats (2 per element)
@@ -129,6 +161,9 @@ struct TcfArgs {
     double *out;           // [batch][6]
     long long sout;
     int n, ldf, ldv;
+    SplitMat Ft;           // when Ft.hi is set: F stored transposed as a split pair, F[r][c] at
+    long long sFt;         // Ft[c*ldft + r], instead of F
+    int ldft;
 };
 cudaError_t cir_launch_tcf(const TcfArgs &t, int batch, cudaStream_t s, int *launches);
 

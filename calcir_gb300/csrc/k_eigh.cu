@@ -481,7 +481,7 @@ __device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb
 // per warp), pv (4 x TB_NB) and stage (aliasing ywall) are shared memory.
 template <int NT, int NMAX>
 __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, int n, int ld, float *d, float *e,
-                                float *tau, float *x, float *ywall, float *pv, float *red) {
+                                float *tau, float *x, float *ywall, float *pv, float *red, unsigned long long *pt) {
     constexpr int NW = NT / 32;
     constexpr int RW = (NMAX + NT - 1) / NT;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -491,6 +491,17 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
     float *ywp = ywall + (size_t)warp * n32;
     for (int i = tid; i < n32; i += NT) x[i] = 0.f;
     __syncthreads();
+    // optional per-phase timers (pt[12..17]), read by thread 0 after a block-wide barrier
+    unsigned long long tlast = (pt && tid == 0) ? globaltimer_ns() : 0ull;
+    auto mark = [&](int slot) {
+        if (!pt) return;
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned long long t = globaltimer_ns();
+            pt[slot] += t - tlast;
+            tlast = t;
+        }
+    };
     const int nref = n - 2;       // columns 0 .. n-3 carry reflectors
     for (int p0 = 0; p0 < nref; p0 += TB_NB) {
         const int nb = min(TB_NB, nref - p0);
@@ -512,6 +523,7 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
                 else { x[r] = v; part += v * v; }
             }
             const float xn2 = block_sum<NT>(part, red);
+            mark(12);
             // (b) the reflector (slarfg convention: v[0] = 1, beta = -sign(alpha)*norm)
             if (tid == 0) {
                 const float alpha = red[48];
@@ -537,6 +549,7 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
             const int j0 = (k + 1) >> 5;
             for (int i = 32 * j0 + lane; i < n32; i += 32) ywp[i] = 0.f;
             __syncthreads();
+            mark(13);
             // (c) y = A22 v on the panel-start trailing block, plus t1 = W^T v, t2 = V^T v
             {
                 const int tt = tn - j0;
@@ -551,6 +564,7 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
                     while (Jj > Ii) { Jj -= Ii + 1; Ii++; }
                 }
             }
+            mark(14);
             for (int dq = warp; dq < 2 * kk; dq += NW) {
                 const float *col = dq < kk ? Wb + (size_t)dq * ld : A + (size_t)(p0 + dq - kk) * ld;
                 float s = 0.f;
@@ -562,6 +576,7 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
                 }
             }
             __syncthreads();
+            mark(15);
             // (d) w = tau (y - V t1 - W t2), then w -= (tau/2)(w.v) v, into column kk of Wb
             float wr[RW];
             float dpart = 0.f;
@@ -588,10 +603,12 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
                 if (r < n) Wb[(size_t)kk * ld + r] = wr[i] + half * x[r];
             }
             __syncthreads();
+            mark(16);
         }
         // (e) the trailing block beyond the panel
         trail_update<NT>(A, Wb, n, ld, p0, nb, ywall);
         __syncthreads();
+        mark(17);
     }
     if (tid == 0) {
         d[n - 2] = A[(size_t)(n - 2) * ld + n - 2];
@@ -628,7 +645,7 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
         // W of the current panel lives in Z, which phase 2 overwrites
         const int n32 = (n + 31) & ~31;
         const int yws = max(n32 * NW, tb_stage(NT));
-        tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red);
+        tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red, pt);
     } else {
         float *vp = U, *wp = U + n4, *vc = U + 2 * n4, *wc = U + 3 * n4;
         bool pending = false;

@@ -1,0 +1,283 @@
+// Propagation step of the split-BF16 mixed form on pre-split operands.
+//
+// The step F <- V exp(i L dt/hbar) V^T F (calcIR.cu:596-613) is two real GEMMs.  Every
+// operand is kept in global memory as a pair of BF16 matrices (hi = bf16(x),
+// lo = bf16(x - hi)), K-major, and each product is hi*hi + hi*lo + lo*hi accumulated in
+// FP32 tensor memory (tcgen05.mma kind::f16):
+//     G = V^T F      A = V (column-major: A(i, k) = V[k][i] at Vc[i*ldh + k]),
+//                    B = F stored transposed (B(k, c) = F[k][c] at Ft[c*ldh + k]),
+//                    epilogue: row i of G times exp(+i w_i dt/hbar), written transposed (Gt)
+//     F' = V G       A = V row-major (Vr[i*ldh + k] = V[i][k]), B = Gt, written as Ft
+// so the output of each product is the K-major operand of the next.  k_split_v writes
+// Vc and Vr from the eigensolver's FP32 eigenvectors once per step.
+//
+// One CTA computes a 128 x 128 tile: thread 0 streams 64-deep K slices of A hi, A lo,
+// B hi and B lo with TMA (cp.async.bulk.tensor, 128-byte swizzle, one 16 KB box each) into
+// a 3-stage ring, counting the bytes on the stage's full barrier; thread 32 issues the
+// 12 MMAs of a stage and commits them to the stage's empty barrier, which the producer
+// waits on before refilling it.  The epilogue reads the accumulator with tcgen05.ld
+// (lane = row) and stores each column's 32 rows of a warp as 64 contiguous bytes.  Every
+// mbarrier wait is bounded; a timeout sets the error flag.
+#include "cir_device.cuh"
+#include "cir_tcgen05.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <mutex>
+
+namespace {
+
+struct SplitMaps {
+    CUtensorMap a_hi, a_lo, b_hi, b_lo;
+};
+
+constexpr int QM = 128, QN = 128, QK = 64;    // tile; K per stage (one 128-byte swizzle row)
+constexpr int QT = 128;                       // threads
+constexpr int QS = 3;                         // stages
+constexpr int Q_TILE = QM * QK * 2;           // one 128 x 64 BF16 tile (16 KB)
+constexpr int Q_STAGE = 4 * Q_TILE;           // A hi, A lo, B hi, B lo
+constexpr size_t Q_SMEM = (size_t)QS * Q_STAGE + 1024 + 256;   // + alignment slack, barriers
+constexpr uint32_t Q_IDESC = make_idesc_mn(1u, QM, QN);   // BF16 operands
+
+// shared-memory descriptor of a K-major tile in the 128-byte swizzled layout (what a TMA
+// box of 64 BF16 x rows with CU_TENSOR_MAP_SWIZZLE_128B writes): 8-row atoms of 1024
+// bytes, stride byte offset 1024, leading byte offset unused (1), layout type 2 at bit 61
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// 3-D tiled TMA load (x = K, y = row, z = matrix) into shared memory, completing on bar
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// One CTA per 128 x 128 tile of C.  Thread 0 is the TMA producer (stage s is refilled once
+// the MMAs that read it have committed to empty[s]), thread 32 issues the MMAs of a stage
+// once full[s] has received its bytes, and all four warps run the epilogue.
+__global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMaps maps, SplitGemmArgs g) {
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    const uint32_t sbase = (raw + 1023) & ~1023u;             // 1024-byte aligned stages
+    unsigned char *smem = smem_raw + (sbase - raw);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + QS * Q_STAGE);   // [QS]
+    uint64_t *empty = full + QS;                                        // [QS]
+    uint64_t *done = empty + QS;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int bz = blockIdx.z;
+    const int m0 = blockIdx.y * QM, n0 = blockIdx.x * QN;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                     "r"(QN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < QS; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+
+    const int KT = (g.K + QK - 1) / QK;
+    bool ok = true;
+    if (tid == 0) {
+        for (int kt = 0; kt < KT && ok; kt++) {
+            const int s = kt % QS;
+            if (kt >= QS) ok = mbar_wait(&empty[s], ((kt / QS) - 1) & 1);
+            if (!ok) break;
+            const uint32_t st = sbase + s * Q_STAGE;
+            mbar_expect_tx(&full[s], Q_STAGE);
+            tma_load3(st, &maps.a_hi, kt * QK, m0, bz, &full[s]);
+            tma_load3(st + Q_TILE, &maps.a_lo, kt * QK, m0, bz, &full[s]);
+            tma_load3(st + 2 * Q_TILE, &maps.b_hi, kt * QK, n0, bz, &full[s]);
+            tma_load3(st + 3 * Q_TILE, &maps.b_lo, kt * QK, n0, bz, &full[s]);
+        }
+    } else if (tid == 32) {
+        for (int kt = 0; kt < KT && ok; kt++) {
+            const int s = kt % QS;
+            ok = mbar_wait(&full[s], (kt / QS) & 1);
+            if (!ok) break;
+            fence_after();
+            const uint32_t st = sbase + s * Q_STAGE;
+            #pragma unroll
+            for (int ks = 0; ks < QK / 16; ks++) {
+                const uint32_t o = 32 * ks;                  // 16 BF16 of K inside the swizzled row
+                const uint64_t ah = desc_sw128(st + o), al = desc_sw128(st + Q_TILE + o);
+                const uint64_t bh = desc_sw128(st + 2 * Q_TILE + o), bl = desc_sw128(st + 3 * Q_TILE + o);
+                mma_f16(tmem, ah, bh, Q_IDESC, (kt | ks) != 0);
+                mma_f16(tmem, ah, bl, Q_IDESC, 1u);
+                mma_f16(tmem, al, bh, Q_IDESC, 1u);
+            }
+            mma_commit(&empty[s]);
+        }
+        mma_commit(done);   // arrives once every MMA issued above has completed
+    }
+    __syncwarp();
+    ok = mbar_wait(done, 0) && ok;
+    fence_after();
+    if (!ok) {
+        if (g.err && lane == 0) atomicExch(g.err, 1);
+    } else {
+        const int r = m0 + warp * 32 + lane;
+        float cph = 1.f, sph = 0.f;
+        if (g.epilogue == 1 && r < g.M) {
+            const float ph = g.w[(size_t)bz * g.wstride + r] * g.dt_over_hbar;
+            sincosf(ph, &sph, &cph);
+        }
+        __nv_bfloat16 *Ch = g.Chi + (size_t)bz * g.sC, *Cl = g.Clo + (size_t)bz * g.sC;
+        #pragma unroll 1
+        for (int c0 = 0; c0 < QN; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (r >= g.M) continue;
+            if (g.epilogue == 1) {
+                #pragma unroll
+                for (int q = 0; q < 16; q += 2) {
+                    const float re = v[q], im = v[q + 1];
+                    v[q] = cph * re - sph * im;
+                    v[q + 1] = sph * re + cph * im;
+                }
+            }
+            #pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int c = n0 + c0 + q;
+                if (c < g.N) {
+                    const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
+                    Ch[(size_t)c * g.ldc + r] = h;
+                    Cl[(size_t)c * g.ldc + r] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+                }
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(QN));
+    }
+}
+
+// Vc = V and Vr = V^T as BF16 hi/lo pairs; V column-major (V[k][i] at A[i*ld + k]).
+// 32 x 32 tiles through shared memory, block (32, 8).
+__global__ void k_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh, long long sV) {
+    __shared__ float t[32][33];
+    const int b = blockIdx.z;
+    const int i0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+    const float *a = A + (size_t)b * sA;
+    const size_t ob = (size_t)b * sV;
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int i = i0 + y, k = k0 + threadIdx.x;
+        float x = 0.f;
+        if (i < n && k < n) {
+            x = a[(size_t)i * ld + k];
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            Vc.hi[ob + (size_t)i * ldh + k] = h;
+            Vc.lo[ob + (size_t)i * ldh + k] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
+        t[y][threadIdx.x] = x;
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += 8) {
+        const int k = k0 + y, i = i0 + threadIdx.x;     // Vr[k][i] = V[k][i] = A[i*ld + k]
+        if (i < n && k < n) {
+            const float x = t[threadIdx.x][y];
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            Vr.hi[ob + (size_t)k * ldh + i] = h;
+            Vr.lo[ob + (size_t)k * ldh + i] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
+    }
+}
+
+// Ft = I: F[r][c] = 1 for c = 2r (the real part of the diagonal), stored at Ft[c*ldh + r].
+__global__ void k_identity_t(SplitMat F, int n, int ldh, long long sF) {
+    const size_t ob = (size_t)blockIdx.y * sF;
+    const int c = blockIdx.x;
+    const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
+    for (int r = threadIdx.x; r < ldh; r += blockDim.x) {
+        F.hi[ob + (size_t)c * ldh + r] = (c == 2 * r) ? one : zero;
+        F.lo[ob + (size_t)c * ldh + r] = zero;
+    }
+}
+
+}  // namespace
+
+size_t cir_split_ld(int n) { return (size_t)((n + 7) & ~7); }
+
+// cuTensorMapEncodeTiled from the driver, looked up once
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// Tensor map of one K-major BF16 operand: x = K (contiguous), y = rows (stride ld), z = matrix
+// (stride sb); boxes of 64 x 128 x 1 in the 128-byte swizzle, zero fill outside.
+static bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int K, int rows, int ld, long long sb, int batch) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dim[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)batch};
+    const cuuint64_t stride[2] = {(cuuint64_t)ld * 2, (cuuint64_t)sb * 2};
+    const cuuint32_t box[3] = {QK, QM, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dim, stride, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches) {
+    if (batch < 1 || batch > 65535 || g.M < 1 || g.N < 1 || g.K < 1 || (g.epilogue == 1 && (g.N & 1)))
+        return cudaErrorInvalidValue;
+    if ((g.lda & 7) || (g.ldb & 7) || (g.sA & 7) || (g.sB & 7) || g.lda < g.K || g.ldb < g.K) return cudaErrorInvalidValue;
+    if ((long long)g.lda * g.M > g.sA && batch > 1) return cudaErrorInvalidValue;
+    if ((long long)g.ldb * g.N > g.sB && batch > 1) return cudaErrorInvalidValue;
+    for (const void *p : {(const void *)g.Ahi, (const void *)g.Alo, (const void *)g.Bhi, (const void *)g.Blo})
+        if (reinterpret_cast<uintptr_t>(p) & 15) return cudaErrorInvalidValue;
+    SplitMaps maps;
+    const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
+    if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch) || !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch) ||
+        !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch) || !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch))
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_tc_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q_SMEM);
+    if (e != cudaSuccess) return e;
+    dim3 grid((g.N + QN - 1) / QN, (g.M + QM - 1) / QM, batch);
+    k_tc_split<<<grid, QT, Q_SMEM, s>>>(maps, g);
+    if (launches) *launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t cir_launch_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh,
+                               long long sV, int batch, cudaStream_t s, int *launches) {
+    dim3 grid((n + 31) / 32, (n + 31) / 32, batch);
+    k_split_v<<<grid, dim3(32, 8), 0, s>>>(A, ld, sA, n, Vc, Vr, ldh, sV);
+    if (launches) *launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t cir_launch_identity_t(SplitMat F, int n, int ldh, long long sF, int batch, cudaStream_t s, int *launches) {
+    k_identity_t<<<dim3(2 * n, batch), 256, 0, s>>>(F, n, ldh, sF);
+    if (launches) *launches += 1;
+    return cudaGetLastError();
+}
