@@ -11,11 +11,13 @@
 // so the output of each product is the K-major operand of the next.  k_split_v writes
 // Vc and Vr from the eigensolver's FP32 eigenvectors once per step.
 //
-// One CTA computes a 128 x 128 tile: thread 0 streams 64-deep K slices of A hi, A lo,
-// B hi and B lo with TMA (cp.async.bulk.tensor, 128-byte swizzle, one 16 KB box each) into
+// One CTA computes a 128 x 128 tile: thread 0 streams 32-deep K slices of A hi, A lo,
+// B hi and B lo with TMA (cp.async.bulk.tensor, 64-byte swizzle, one 8 KB box each) into
 // a 3-stage ring, counting the bytes on the stage's full barrier; thread 32 issues the
-// 12 MMAs of a stage and commits them to the stage's empty barrier, which the producer
-// waits on before refilling it.  The epilogue reads the accumulator with tcgen05.ld
+// 6 MMAs of a stage and commits them to the stage's empty barrier, which the producer
+// waits on before refilling it.  At 97 KB of shared memory two CTAs share an SM, so one
+// CTA's epilogue overlaps the other's MMAs (measured faster than 64-deep 128-byte-swizzled
+// stages at one CTA per SM).  The epilogue reads the accumulator with tcgen05.ld
 // (lane = row) and stores each column's 32 rows of a warp as 64 contiguous bytes.  Every
 // mbarrier wait is bounded; a timeout sets the error flag.
 #include "cir_device.cuh"
@@ -32,20 +34,26 @@ struct SplitMaps {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
 };
 
-constexpr int QM = 128, QN = 128, QK = 64;    // tile; K per stage (one 128-byte swizzle row)
+constexpr int QM = 128, QN = 128;             // tile
 constexpr int QT = 128;                       // threads
-constexpr int QS = 3;                         // stages
-constexpr int Q_TILE = QM * QK * 2;           // one 128 x 64 BF16 tile (16 KB)
-constexpr int Q_STAGE = 4 * Q_TILE;           // A hi, A lo, B hi, B lo
-constexpr size_t Q_SMEM = (size_t)QS * Q_STAGE + 1024 + 256;   // + alignment slack, barriers
 constexpr uint32_t Q_IDESC = make_idesc_mn(1u, QM, QN);   // BF16 operands
 
-// shared-memory descriptor of a K-major tile in the 128-byte swizzled layout (what a TMA
-// box of 64 BF16 x rows with CU_TENSOR_MAP_SWIZZLE_128B writes): 8-row atoms of 1024
-// bytes, stride byte offset 1024, leading byte offset unused (1), layout type 2 at bit 61
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
-    return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
-           (2ull << 61);
+// QK BF16 of K per stage = one swizzled row of 2 QK bytes (128-byte swizzle for QK = 64,
+// 64-byte for QK = 32), QS stages of A hi, A lo, B hi, B lo
+template <int QK, int QS> struct QCfg {
+    static constexpr int TILE = QM * QK * 2;
+    static constexpr int STAGE = 4 * TILE;
+    static constexpr size_t SMEM = (size_t)QS * STAGE + 1024 + 256;   // + alignment slack, barriers
+    static constexpr uint64_t LAYOUT = QK == 64 ? 2ull : 4ull;         // SWIZZLE_128B / SWIZZLE_64B
+};
+
+// shared-memory descriptor of a K-major tile in the swizzled layout a TMA box of QK BF16
+// x rows writes: 8-row atoms of 16 QK bytes (the stride byte offset), leading byte offset
+// unused (1), the layout type at bit 61
+template <int QK, int QS>
+__device__ __forceinline__ uint64_t desc_sw(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((uint64_t)((16 * QK) >> 4) << 32) | (1ull << 46) |
+           (QCfg<QK, QS>::LAYOUT << 61);
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
@@ -63,7 +71,9 @@ __device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *map, 
 // One CTA per 128 x 128 tile of C.  Thread 0 is the TMA producer (stage s is refilled once
 // the MMAs that read it have committed to empty[s]), thread 32 issues the MMAs of a stage
 // once full[s] has received its bytes, and all four warps run the epilogue.
+template <int QK, int QS>
 __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMaps maps, SplitGemmArgs g) {
+    constexpr int Q_TILE = QCfg<QK, QS>::TILE, Q_STAGE = QCfg<QK, QS>::STAGE;
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
     const uint32_t sbase = (raw + 1023) & ~1023u;             // 1024-byte aligned stages
@@ -118,8 +128,8 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
             #pragma unroll
             for (int ks = 0; ks < QK / 16; ks++) {
                 const uint32_t o = 32 * ks;                  // 16 BF16 of K inside the swizzled row
-                const uint64_t ah = desc_sw128(st + o), al = desc_sw128(st + Q_TILE + o);
-                const uint64_t bh = desc_sw128(st + 2 * Q_TILE + o), bl = desc_sw128(st + 3 * Q_TILE + o);
+                const uint64_t ah = desc_sw<QK, QS>(st + o), al = desc_sw<QK, QS>(st + Q_TILE + o);
+                const uint64_t bh = desc_sw<QK, QS>(st + 2 * Q_TILE + o), bl = desc_sw<QK, QS>(st + 3 * Q_TILE + o);
                 mma_f16(tmem, ah, bh, Q_IDESC, (kt | ks) != 0);
                 mma_f16(tmem, ah, bl, Q_IDESC, 1u);
                 mma_f16(tmem, al, bh, Q_IDESC, 1u);
@@ -219,6 +229,15 @@ __global__ void k_identity_t(SplitMat F, int n, int ldh, long long sF) {
 
 size_t cir_split_ld(int n) { return (size_t)((n + 7) & ~7); }
 
+template <int QK, int QS>
+static cudaError_t launch_split(const SplitMaps &maps, const SplitGemmArgs &g, dim3 grid, cudaStream_t s) {
+    constexpr size_t smem = QCfg<QK, QS>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_tc_split<QK, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_tc_split<QK, QS><<<grid, QT, smem, s>>>(maps, g);
+    return cudaGetLastError();
+}
+
 // cuTensorMapEncodeTiled from the driver, looked up once
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -235,15 +254,16 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // Tensor map of one K-major BF16 operand: x = K (contiguous), y = rows (stride ld), z = matrix
 // (stride sb); boxes of 64 x 128 x 1 in the 128-byte swizzle, zero fill outside.
-static bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int K, int rows, int ld, long long sb, int batch) {
+static bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int K, int rows, int ld, long long sb, int batch, int QK) {
     auto fn = encode_fn();
     if (!fn) return false;
     const cuuint64_t dim[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)batch};
     const cuuint64_t stride[2] = {(cuuint64_t)ld * 2, (cuuint64_t)sb * 2};
-    const cuuint32_t box[3] = {QK, QM, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)QK, QM, 1};
     const cuuint32_t es[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dim, stride, box, es,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, QK == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -255,17 +275,19 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
     if ((long long)g.ldb * g.N > g.sB && batch > 1) return cudaErrorInvalidValue;
     for (const void *p : {(const void *)g.Ahi, (const void *)g.Alo, (const void *)g.Bhi, (const void *)g.Blo})
         if (reinterpret_cast<uintptr_t>(p) & 15) return cudaErrorInvalidValue;
+    constexpr int QK = 32, QS = 3;   // 64-byte swizzle, 3 x 32 KB stages: two CTAs per SM
     SplitMaps maps;
     const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
-    if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch) || !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch) ||
-        !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch) || !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch))
+    if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK) ||
+        !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch, QK) ||
+        !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK) ||
+        !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK))
         return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_tc_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q_SMEM);
-    if (e != cudaSuccess) return e;
     dim3 grid((g.N + QN - 1) / QN, (g.M + QM - 1) / QM, batch);
-    k_tc_split<<<grid, QT, Q_SMEM, s>>>(maps, g);
+    const cudaError_t e = launch_split<QK, QS>(maps, g, grid, s);
+    if (e != cudaSuccess) return e;
     if (launches) *launches += 1;
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 cudaError_t cir_launch_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh,
