@@ -31,7 +31,7 @@
 namespace {
 
 constexpr int DC_LEAF = 32;
-constexpr int DC_NT = 256;          // threads of a merge block
+constexpr int DC_NT = 256;          // threads of a merge block of more than 128 rows (fewer below)
 constexpr float DC_EPS = 5.9604645e-8f;   // 2^-24
 
 __host__ __device__ inline int dc_off(int level, int b, int n) { return (int)(((long long)b * n) >> level); }
@@ -152,23 +152,25 @@ struct DcSmem {      // offsets (floats) of the merge block's arrays for a merge
     }
 };
 
+template <int NT>
 __device__ float dc_block_max(float v, float *red) {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     __syncthreads();
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
     float r = 0.f;
-    for (int w = 0; w < DC_NT / 32; w++) r = fmaxf(r, red[w]);
+    for (int w = 0; w < NT / 32; w++) r = fmaxf(r, red[w]);
     return r;
 }
 
+template <int NT>
 __device__ float dc_block_sum(float v, float *red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();
     if ((threadIdx.x & 31) == 0) red[32 + (threadIdx.x >> 5)] = v;
     __syncthreads();
     float r = 0.f;
-    for (int w = 0; w < DC_NT / 32; w++) r += red[32 + w];
+    for (int w = 0; w < NT / 32; w++) r += red[32 + w];
     return r;
 }
 
@@ -230,7 +232,8 @@ __device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rh
     return o;
 }
 
-__global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int KM, const float *Qin, float *Mscr,
+template <int NT>
+__global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, const float *Qin, float *Mscr,
                                                     float *Uout) {
     extern __shared__ __align__(16) float sm[];
     const DcSmem L(KM);
@@ -254,12 +257,12 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
     const float rho = 2.f * fabsf(beta);
     const float sgn = beta >= 0.f ? 1.f : -1.f;
     // z and the two sorted lists
-    for (int i = tid; i < K; i += DC_NT) {
+    for (int i = tid; i < K; i += NT) {
         D[i] = dw[a0 + i];
         zs[i] = (i < k1 ? Q[(size_t)(a0 + i) * ld + mid - 1] : sgn * Q[(size_t)(a0 + i) * ld + mid]) * 0.70710678118654752f;
     }
     __syncthreads();
-    for (int i = tid; i < K; i += DC_NT) {
+    for (int i = tid; i < K; i += NT) {
         int rnk;
         const float v = D[i];
         if (i < k1) {   // number of D2 < v
@@ -275,15 +278,15 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
     }
     __syncthreads();
     float mx = 0.f;
-    for (int r = tid; r < K; r += DC_NT) {
+    for (int r = tid; r < K; r += NT) {
         const int i = perm[r];
         Ds[r] = D[i];
         z2[r] = zs[i];       // z in sorted order (z2 reused below for z^2)
         mx = fmaxf(mx, fmaxf(fabsf(D[i]), fabsf(zs[i])));
     }
-    const float tol = 8.f * DC_EPS * dc_block_max(mx, red);
+    const float tol = 8.f * DC_EPS * dc_block_max<NT>(mx, red);
     __syncthreads();
-    for (int r = tid; r < K; r += DC_NT) zs[r] = z2[r];
+    for (int r = tid; r < K; r += NT) zs[r] = z2[r];
     __syncthreads();
     // deflation (LAPACK laed2): sequential scan over the sorted entries
     if (tid == 0) {
@@ -323,7 +326,7 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
     __syncthreads();
     const int Kp = s_kp, nrot = s_m, nd = s_nd;
     float zpart = 0.f;
-    for (int i = tid; i < Kp; i += DC_NT) {
+    for (int i = tid; i < Kp; i += NT) {
         const int r = nidx[i];
         Dn[i] = Ds[r];
         const float zz = zs[r];
@@ -331,17 +334,17 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
         zh[i] = zz;          // sign carrier until the recomputation below
         zpart += zz * zz;
     }
-    const float z2sum = dc_block_sum(zpart, red);
+    const float z2sum = dc_block_sum<NT>(zpart, red);
     __syncthreads();
     // secular roots
-    for (int i = tid; i < Kp; i += DC_NT) {
+    for (int i = tid; i < Kp; i += NT) {
         float t;
         org[i] = dc_root(i, Kp, Dn, z2, rho, z2sum, &t);
         tau[i] = t;
     }
     __syncthreads();
     // Gu-Eisenstat: zh_j^2 = -prod_i (Dn_j - lambda_i) / prod_{i != j} (Dn_j - Dn_i)
-    for (int j = tid; j < Kp; j += DC_NT) {
+    for (int j = tid; j < Kp; j += NT) {
         const float dj = Dn[j];
         float p = (dj - Dn[org[j]]) - tau[j];
         for (int i = 0; i < Kp; i++)
@@ -349,9 +352,9 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
         vals[j] = copysignf(sqrtf(fmaxf(-p, 0.f)), zh[j]);
     }
     __syncthreads();
-    for (int j = tid; j < Kp; j += DC_NT) zh[j] = vals[j];
+    for (int j = tid; j < Kp; j += NT) zh[j] = vals[j];
     __syncthreads();
-    for (int i = tid; i < Kp; i += DC_NT) {
+    for (int i = tid; i < Kp; i += NT) {
         const float base = Dn[org[i]], ti = tau[i];
         float sq = 0.f;
         for (int j = 0; j < Kp; j++) {
@@ -361,9 +364,9 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
         inv[i] = 1.f / sqrtf(sq);
     }
     // eigenvalues: roots then deflated values; ascending rank (ties by index)
-    for (int q = tid; q < K; q += DC_NT) vals[q] = q < Kp ? Dn[org[q]] + tau[q] : Ds[defl[q - Kp]];
+    for (int q = tid; q < K; q += NT) vals[q] = q < Kp ? Dn[org[q]] + tau[q] : Ds[defl[q - Kp]];
     __syncthreads();
-    for (int q = tid; q < K; q += DC_NT) {
+    for (int q = tid; q < K; q += NT) {
         const float v = vals[q];
         int r = 0;
         for (int i = 0; i < K; i++) r += (vals[i] < v) || (vals[i] == v && i < q);
@@ -371,8 +374,25 @@ __global__ void __launch_bounds__(DC_NT) k_dc_merge(EighArgs a, int level, int K
         dw[a0 + r] = v;
     }
     __syncthreads();
-    // M = G W in the sorted basis (row-major), then U = P M
-    for (int c = tid; c < K; c += DC_NT) {
+    // M = G W in the sorted basis (row-major), then U = P M; without deflation rotations
+    // (G = I) the columns go straight to U
+    if (nrot == 0) {
+        for (int c = tid; c < K; c += NT) {
+            const int q = src[c];
+            if (q < Kp) {
+                const float base = Dn[org[q]], ti = tau[q], sc = inv[q];
+                for (int r = 0; r < K; r++) {
+                    const int jn = kind[r];
+                    U[(size_t)(a0 + perm[r]) * ld + a0 + c] = jn >= 0 ? zh[jn] / ((Dn[jn] - base) - ti) * sc : 0.f;
+                }
+            } else {
+                const int p = defl[q - Kp];
+                for (int r = 0; r < K; r++) U[(size_t)(a0 + perm[r]) * ld + a0 + c] = r == p ? 1.f : 0.f;
+            }
+        }
+        return;
+    }
+    for (int c = tid; c < K; c += NT) {
         const int q = src[c];
         if (q < Kp) {
             const float base = Dn[org[q]], ti = tau[q], sc = inv[q];
@@ -520,10 +540,16 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
         const int KM = ((n + (1 << level) - 1) >> level);
         const DcSmem L(KM);
         const size_t smem = sizeof(float) * L.total;
-        e = cudaFuncSetAttribute(k_dc_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
         const int other = cur ^ 1;
-        k_dc_merge<<<dim3(1 << level, nmat), DC_NT, smem, s>>>(a, level, KM, buf[cur], buf[other], buf[2]);
+        // small merges in small blocks, so that many of them share an SM
+        auto merge = [&](auto kern, int nt) -> cudaError_t {
+            cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (r != cudaSuccess) return r;
+            kern<<<dim3(1 << level, nmat), nt, smem, s>>>(a, level, KM, buf[cur], buf[other], buf[2]);
+            return cudaSuccess;
+        };
+        e = KM <= 64 ? merge(k_dc_merge<64>, 64) : KM <= 128 ? merge(k_dc_merge<128>, 128) : merge(k_dc_merge<DC_NT>, DC_NT);
+        if (e != cudaSuccess) return e;
         // the top two levels of the mixed forms on the tensor cores: one batched product per
         // merge half when every offset keeps 16-byte alignment
         bool tc = a.precision != CIR_PREC_FP32 && level <= 1;
