@@ -91,9 +91,10 @@ size_t cir_eigh_de_bytes(int ld);
 size_t cir_dc_bytes(int n, int ld);
 cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
 // V = Q_H Q into a.A by blocked compact-WY application of the tridiagonalisation's
-// reflectors (in a.A) to Q; Q is overwritten, P is scratch (a.mstride floats per matrix),
-// a.Z holds the blocks' T^T V^T.
-cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, int nmat, cudaStream_t s, int *launches);
+// reflectors (in a.A) to Q; Q is overwritten, P and U are scratch (a.mstride floats per
+// matrix), a.Z holds the blocks' T^T V^T.
+cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, float *U, int nmat, cudaStream_t s,
+                                     int *launches);
 int cir_eigh_max_n();
 
 // batched SIMT FP32 GEMM, C = A * B (row-major B, C); A row- or column-major.
@@ -128,12 +129,19 @@ struct SplitMat {
     __nv_bfloat16 *hi, *lo;
 };
 // C = A B (hi*hi + hi*lo + lo*hi, FP32 accumulation) with K-major operands:
-// A(i, k) at A[i*lda + k], B(k, j) at B[j*ldb + k]; C(i, j) written as hi/lo at C[j*ldc + i].
+// A(i, k) at A[i*lda + k], B(k, j) at B[j*ldb + k].  out_mode 0: C(i, j) written as a
+// hi/lo pair at C[j*ldc + i]; 1: as a pair at C[i*ldc + j]; 2: in FP32 at Cf[i*ldc + j].
 // lda, ldb and the batch strides are multiples of 8, the operand pointers 16-byte aligned.
-// epilogue 1: columns (2q, 2q+1) of row i rotated by exp(+i w[i] dt/hbar) before the split.
+// epilogue 1: columns (2q, 2q+1) of row i rotated by exp(+i w[i] dt/hbar) before the split;
+// epilogue 2: C = D - A B, D a row-major pair (D[i*ldd + j], batch stride sD; may be C).
 struct SplitGemmArgs {
     const __nv_bfloat16 *Ahi, *Alo, *Bhi, *Blo;
     __nv_bfloat16 *Chi, *Clo;
+    float *Cf;
+    int out_mode;
+    const __nv_bfloat16 *Dhi, *Dlo;
+    int ldd;
+    long long sD;
     int M, N, K;
     int lda, ldb, ldc;
     long long sA, sB, sC;

@@ -63,7 +63,21 @@ __device__ __forceinline__ void bt_stage(float *A, int ld, int n, int kb, int nb
     }
 }
 
-__global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a) {
+// Outputs of the split form of the prep (the mixed forms): V_b and Y_b^T as BF16 hi/lo pairs.
+struct BtSplit {
+    SplitMat V;        // V[(kb + j)*ldq + r]: column kb + j of the cleaned reflectors, rows kb..
+    SplitMat Yt;       // block b at Yt + bt_yoff(b, n, ldy): Y_b^T, (n - kb) rows of ldy
+    int ldq, ldy;      // ldy = min(BT_NB, n - 2 rounded up to 8): the width of a block
+    long long sV, sY;  // per-matrix strides (elements)
+};
+
+// offset of block b's Y_b^T: the (n - kb') x ldy blocks of the blocks before it
+__host__ __device__ inline long long bt_yoff(int b, int n, int ldy) {
+    return (long long)ldy * ((long long)b * n - (long long)BT_NB * b * (b - 1) / 2);
+}
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a, BtSplit sp) {
     extern __shared__ __align__(16) float bsm[];
     float *M = bsm;                           // [BT_NB][BT_LDM]: G, then T^T (M[j][i] = T[i][j])
     float *Vt = M + BT_NB * BT_LDM;           // [BT_NB][BT_LDV]
@@ -86,8 +100,21 @@ __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a) {
             for (int q = 0; q < 8; q++) acc[p][q] = 0.f;
         for (int r0 = kb; r0 < n; r0 += BT_RC) {
             __syncthreads();
-            bt_stage(A, ld, n, kb, nbb, r0, true, Vt);
+            bt_stage(A, ld, n, kb, nbb, r0, !SPLIT, Vt);
             __syncthreads();
+            if (SPLIT) {   // the cleaned chunk as a split pair: column kb + j, rows r0..
+                const size_t ov = (size_t)mat * sp.sV;
+                for (int idx = t; idx < BT_NB * BT_RC; idx += BT_NT) {
+                    const int j = idx / BT_RC, rr = idx - j * BT_RC, r = r0 + rr;
+                    if (j < nbb && r < n) {
+                        const float x = Vt[j * BT_LDV + rr];
+                        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                        const size_t o = ov + (size_t)(kb + j) * sp.ldq + r;
+                        sp.V.hi[o] = h;
+                        sp.V.lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+                    }
+                }
+            }
             #pragma unroll 1
             for (int rr = 0; rr < BT_RC; rr += 4) {
                 float4 va[8];
@@ -154,40 +181,143 @@ __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a) {
                 }
             }
         }
-        const int r = r0 + 4 * tr;
-        #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int j = tj + 16 * q;
-            if (j >= nbb) continue;
-            float *y = Y + (size_t)(kb + j) * ld + r;
-            if (r + 3 < n) {
-                *reinterpret_cast<float4 *>(y) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
-            } else {
+        if (SPLIT) {
+            // Y_b^T rows r0..r0+63 through shared memory (Vt is free once every thread has
+            // its products), then 32 values of one row per thread as a split pair
+            __syncthreads();
+            float *Ts = Vt;   // [BT_RC][BT_NB + 1]
+            #pragma unroll
+            for (int q = 0; q < 8; q++)
                 #pragma unroll
-                for (int c = 0; c < 4; c++)
-                    if (r + c < n) y[c] = acc[q][c];
+                for (int c = 0; c < 4; c++) Ts[(4 * tr + c) * (BT_NB + 1) + tj + 16 * q] = acc[q][c];
+            __syncthreads();
+            const int rl = t >> 2, j0 = (t & 3) * 32, r = r0 + rl;
+            if (r < n) {
+                const size_t o = (size_t)mat * sp.sY + bt_yoff(blockIdx.x, n, sp.ldy) + (size_t)(r - kb) * sp.ldy + j0;
+                #pragma unroll
+                for (int q = 0; q < 32; q += 8) {
+                    if (j0 + q >= sp.ldy) break;
+                    uint32_t ph[4], pl[4];
+                    #pragma unroll
+                    for (int u = 0; u < 8; u += 2) {
+                        const float x0 = j0 + q + u < nbb ? Ts[rl * (BT_NB + 1) + j0 + q + u] : 0.f;
+                        const float x1 = j0 + q + u + 1 < nbb ? Ts[rl * (BT_NB + 1) + j0 + q + u + 1] : 0.f;
+                        const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+                        const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+                        const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+                        ph[u / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                        pl[u / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                    }
+                    *reinterpret_cast<uint4 *>(sp.Yt.hi + o + q) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+                    *reinterpret_cast<uint4 *>(sp.Yt.lo + o + q) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+                }
+            }
+        } else {
+            const int r = r0 + 4 * tr;
+            #pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int j = tj + 16 * q;
+                if (j >= nbb) continue;
+                float *y = Y + (size_t)(kb + j) * ld + r;
+                if (r + 3 < n) {
+                    *reinterpret_cast<float4 *>(y) = make_float4(acc[q][0], acc[q][1], acc[q][2], acc[q][3]);
+                } else {
+                    #pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        if (r + c < n) y[c] = acc[q][c];
+                }
             }
         }
     }
 }
 
+// Q as a split pair in the same layout (column c at Q[c*ld ..], rows 0..n-1).
+__global__ void k_bt_split_q(const float *Q, long long sQ, int n, int ld, SplitMat Qs, long long sS) {
+    const int c = blockIdx.x, mat = blockIdx.y;
+    const float *q = Q + (size_t)mat * sQ + (size_t)c * ld;
+    const size_t o = (size_t)mat * sS + (size_t)c * ld;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        const float x = q[r];
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        Qs.hi[o + r] = h;
+        Qs.lo[o + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+}
+
 }  // namespace
 
+// The mixed forms with ld a multiple of 8: every operand as a BF16 split pair and the
+// products on the pre-split tensor-core GEMM (k_tc_split.cu).  Q is first split into Qs
+// (in P's buffer); the prep writes V_b (into Q's buffer) and Y_b^T (into a.Z) as pairs; P_b
+// goes to U; the updates of Qs stay split and the last one writes V in FP32 into a.A.
+static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, float *U, int nmat, int nblk,
+                                       cudaStream_t s, int &nl) {
+    const int n = a.n, ld = a.ld, nrefl = n - 2;
+    const long long ms = a.mstride, ss = 2 * a.mstride;   // per-matrix stride of a pair (BF16 elements)
+    auto pair = [&](float *buf) {
+        __nv_bfloat16 *b = reinterpret_cast<__nv_bfloat16 *>(buf);
+        return SplitMat{b, b + ms};
+    };
+    const SplitMat Qs = pair(P), Vs = pair(Q), Ys = pair(a.Z), Ps = pair(U);
+    k_bt_split_q<<<dim3(n, nmat), 256, 0, s>>>(Q, ms, n, ld, Qs, ss);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const size_t smem = bt_prep_smem();
+    if ((e = cudaFuncSetAttribute(k_bt_prep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return e;
+    const int bw = min(BT_NB, (nrefl + 7) & ~7);   // width of P and of the Y_b^T blocks (<= ld)
+    BtSplit sp{Vs, Ys, ld, bw, ss, ss};
+    k_bt_prep<true><<<dim3(nblk, nmat), BT_NT, smem, s>>>(a, sp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    nl += 2;
+    for (int b = nblk - 1; b >= 0; b--) {
+        const int kb = b * BT_NB, nbb = min(BT_NB, nrefl - kb), m = n - kb;
+        SplitGemmArgs g1{};                                        // P = Z^T[:, kb:] V_b
+        g1.Ahi = Qs.hi + kb; g1.Alo = Qs.lo + kb; g1.lda = ld; g1.sA = ss;
+        g1.Bhi = Vs.hi + (size_t)kb * ld + kb; g1.Blo = Vs.lo + (size_t)kb * ld + kb; g1.ldb = ld; g1.sB = ss;
+        g1.Chi = Ps.hi; g1.Clo = Ps.lo; g1.ldc = bw; g1.sC = ss; g1.out_mode = 1;
+        g1.M = n; g1.N = nbb; g1.K = m;
+        g1.err = a.err;
+        SplitGemmArgs g2{};                                        // Z^T[:, kb:] -= P Y_b
+        g2.Ahi = Ps.hi; g2.Alo = Ps.lo; g2.lda = bw; g2.sA = ss;
+        g2.Bhi = Ys.hi + bt_yoff(b, n, bw); g2.Blo = Ys.lo + bt_yoff(b, n, bw); g2.ldb = bw; g2.sB = ss;
+        g2.epilogue = 2;
+        g2.Dhi = Qs.hi + kb; g2.Dlo = Qs.lo + kb; g2.ldd = ld; g2.sD = ss;
+        if (b > 0) {
+            g2.Chi = Qs.hi + kb; g2.Clo = Qs.lo + kb; g2.ldc = ld; g2.sC = ss; g2.out_mode = 1;
+        } else {
+            g2.Cf = a.A; g2.ldc = ld; g2.sC = ms; g2.out_mode = 2;
+        }
+        g2.M = n; g2.N = m; g2.K = nbb;
+        g2.err = a.err;
+        if ((e = cir_launch_split_gemm(g1, nmat, s, &nl)) != cudaSuccess) return e;
+        if ((e = cir_launch_split_gemm(g2, nmat, s, &nl)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // V = Q_H Q into a.A.  Q (the tridiagonal eigenvectors, column-major, a.mstride per
-// matrix) is overwritten; P is scratch of a.mstride floats per matrix; a.Z receives Y.
+// matrix) is overwritten; P and U are scratch of a.mstride floats per matrix; a.Z receives Y.
 // a.A must hold the reflectors of the tridiagonalisation.
-cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, int nmat, cudaStream_t s, int *launches) {
+cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, float *U, int nmat, cudaStream_t s,
+                                     int *launches) {
     const int n = a.n, ld = a.ld, nrefl = n - 2;
     if ((ld & 3) || (reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15))
         return cudaErrorInvalidValue;
     if (nrefl <= 0)
         return cudaMemcpyAsync(a.A, Q, sizeof(float) * (size_t)nmat * a.mstride, cudaMemcpyDeviceToDevice, s);
     const int nblk = (nrefl + BT_NB - 1) / BT_NB;
+    if (a.precision == CIR_PREC_BF16X3 && (ld & 7) == 0) {
+        int nl = 0;
+        const cudaError_t e = backtransform_split(a, Q, P, U, nmat, nblk, s, nl);
+        if (launches) *launches += nl;
+        return e;
+    }
     const int pld = min(BT_NB, (nrefl + 3) & ~3);   // P: n x pld, pld <= ld
     const size_t smem = bt_prep_smem();
-    cudaError_t e = cudaFuncSetAttribute(k_bt_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_bt_prep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bt_prep<<<dim3(nblk, nmat), BT_NT, smem, s>>>(a);
+    k_bt_prep<false><<<dim3(nblk, nmat), BT_NT, smem, s>>>(a, BtSplit{});
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     int nl = 1;
     for (int b = nblk - 1; b >= 0; b--) {

@@ -31,7 +31,7 @@
 namespace {
 
 constexpr int DC_LEAF = 32;
-constexpr int DC_NT = 256;          // threads of a merge block of more than 128 rows (fewer below)
+constexpr int DC_NT = 256;          // threads of a merge block of 129-512 rows (fewer below, twice above)
 constexpr float DC_EPS = 5.9604645e-8f;   // 2^-24
 
 __host__ __device__ inline int dc_off(int level, int b, int n) { return (int)(((long long)b * n) >> level); }
@@ -197,8 +197,9 @@ __device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rh
         float psi = 0.f, phi = 0.f, dpsi = 0.f, dphi = 0.f, di = 0.f, dj = 0.f;
         for (int j = 0; j < Kp; j++) {
             const float dl = (Dn[j] - dorg) - t;
-            const float q = z2[j] / dl;
-            const float dq = q / dl;
+            const float rl = __frcp_rn(dl);   // one correctly rounded reciprocal per term
+            const float q = z2[j] * rl;
+            const float dq = q * rl;
             if (j <= ip) { psi += q; dpsi += dq; }
             else { phi += q; dphi += dq; }
             if (j == ip) di = dl;
@@ -548,7 +549,8 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
             kern<<<dim3(1 << level, nmat), nt, smem, s>>>(a, level, KM, buf[cur], buf[other], buf[2]);
             return cudaSuccess;
         };
-        e = KM <= 64 ? merge(k_dc_merge<64>, 64) : KM <= 128 ? merge(k_dc_merge<128>, 128) : merge(k_dc_merge<DC_NT>, DC_NT);
+        e = KM <= 64 ? merge(k_dc_merge<64>, 64) : KM <= 128 ? merge(k_dc_merge<128>, 128)
+          : KM <= 512 ? merge(k_dc_merge<DC_NT>, DC_NT) : merge(k_dc_merge<2 * DC_NT>, 2 * DC_NT);
         if (e != cudaSuccess) return e;
         // the top two levels of the mixed forms on the tensor cores: one batched product per
         // merge half when every offset keeps 16-byte alignment
@@ -591,7 +593,7 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
     }
     // V = Q_H Q_T into a.A: the reflectors applied to Q_T (buf[cur]) in compact WY blocks,
     // with the free ping-pong buffer as scratch
-    e = cir_launch_backtransform(a, buf[cur], buf[cur ^ 1], nmat, s, &nl);
+    e = cir_launch_backtransform(a, buf[cur], buf[cur ^ 1], buf[2], nmat, s, &nl);
     if (e != cudaSuccess) return e;
     k_dc_finish<<<nmat, 256, 0, s>>>(a);
     nl += 1;

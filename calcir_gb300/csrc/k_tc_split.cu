@@ -164,13 +164,72 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
                     v[q + 1] = sph * re + cph * im;
                 }
             }
-            #pragma unroll
-            for (int q = 0; q < 16; q++) {
-                const int c = n0 + c0 + q;
-                if (c < g.N) {
-                    const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
-                    Ch[(size_t)c * g.ldc + r] = h;
-                    Cl[(size_t)c * g.ldc + r] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+            const int c = n0 + c0;
+            if (g.epilogue == 2) {   // C = D - A B, D a row-major split pair
+                const __nv_bfloat16 *dh = g.Dhi + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                const __nv_bfloat16 *dl = g.Dlo + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(dh) | reinterpret_cast<uintptr_t>(dl)) & 15) == 0) {
+                    #pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const uint4 a = *reinterpret_cast<const uint4 *>(dh + 8 * h);
+                        const uint4 b = *reinterpret_cast<const uint4 *>(dl + 8 * h);
+                        const uint32_t wa[4] = {a.x, a.y, a.z, a.w}, wb[4] = {b.x, b.y, b.z, b.w};
+                        #pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            const float xh = __uint_as_float((wa[u / 2] >> (16 * (u & 1))) << 16);
+                            const float xl = __uint_as_float((wb[u / 2] >> (16 * (u & 1))) << 16);
+                            v[8 * h + u] = (xh + xl) - v[8 * h + u];
+                        }
+                    }
+                } else {
+                    #pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        v[q] = (c + q < g.N ? __bfloat162float(dh[q]) + __bfloat162float(dl[q]) : 0.f) - v[q];
+                }
+            }
+            if (g.out_mode == 0) {           // transposed split pair
+                #pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    if (c + q < g.N) {
+                        const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
+                        Ch[(size_t)(c + q) * g.ldc + r] = h;
+                        Cl[(size_t)(c + q) * g.ldc + r] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+                    }
+                }
+            } else if (g.out_mode == 1) {    // row-major split pair
+                uint32_t wh[8], wl[8];   // 16 values as packed BF16 pairs
+                #pragma unroll
+                for (int q = 0; q < 16; q += 2) {
+                    const __nv_bfloat16 h0 = __float2bfloat16_rn(v[q]), h1 = __float2bfloat16_rn(v[q + 1]);
+                    const __nv_bfloat16 l0 = __float2bfloat16_rn(v[q] - __bfloat162float(h0));
+                    const __nv_bfloat16 l1 = __float2bfloat16_rn(v[q + 1] - __bfloat162float(h1));
+                    wh[q / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                    wl[q / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                }
+                __nv_bfloat16 *ph = Ch + (size_t)r * g.ldc + c, *pl = Cl + (size_t)r * g.ldc + c;
+                if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(ph) | reinterpret_cast<uintptr_t>(pl)) & 15) == 0) {
+                    #pragma unroll
+                    for (int q = 0; q < 8; q += 4) {
+                        *reinterpret_cast<uint4 *>(ph + 2 * q) = make_uint4(wh[q], wh[q + 1], wh[q + 2], wh[q + 3]);
+                        *reinterpret_cast<uint4 *>(pl + 2 * q) = make_uint4(wl[q], wl[q + 1], wl[q + 2], wl[q + 3]);
+                    }
+                } else {
+                    #pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        if (c + q < g.N) {
+                            ph[q] = __ushort_as_bfloat16((unsigned short)(wh[q / 2] >> (16 * (q & 1))));
+                            pl[q] = __ushort_as_bfloat16((unsigned short)(wl[q / 2] >> (16 * (q & 1))));
+                        }
+                }
+            } else {                         // row-major FP32
+                float *pf = g.Cf + (size_t)bz * g.sC + (size_t)r * g.ldc + c;
+                if (c + 15 < g.N && (reinterpret_cast<uintptr_t>(pf) & 15) == 0) {
+                    #pragma unroll
+                    for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4 *>(pf + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                } else {
+                    #pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        if (c + q < g.N) pf[q] = v[q];
                 }
             }
         }
@@ -275,7 +334,8 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
     if ((long long)g.ldb * g.N > g.sB && batch > 1) return cudaErrorInvalidValue;
     for (const void *p : {(const void *)g.Ahi, (const void *)g.Alo, (const void *)g.Bhi, (const void *)g.Blo})
         if (reinterpret_cast<uintptr_t>(p) & 15) return cudaErrorInvalidValue;
-    constexpr int QK = 32, QS = 3;   // 64-byte swizzle, 3 x 32 KB stages: two CTAs per SM
+    constexpr int QK = 32;   // 64-byte swizzle; 3 x 32 KB stages (two CTAs per SM), or for
+                             // products of at most 4 K slices 2 stages (three CTAs per SM)
     SplitMaps maps;
     const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
     if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK) ||
@@ -284,7 +344,7 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
         !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK))
         return cudaErrorInvalidValue;
     dim3 grid((g.N + QN - 1) / QN, (g.M + QM - 1) / QM, batch);
-    const cudaError_t e = launch_split<QK, QS>(maps, g, grid, s);
+    const cudaError_t e = g.K <= 4 * QK ? launch_split<QK, 2>(maps, g, grid, s) : launch_split<QK, 3>(maps, g, grid, s);
     if (e != cudaSuccess) return e;
     if (launches) *launches += 1;
     return cudaSuccess;
