@@ -43,6 +43,7 @@ class Params(C.Structure):
         ("synth_sigma_trans", C.c_float), ("synth_sigma_rot", C.c_float),
         ("precision", C.c_int), ("batch_frames", C.c_int), ("verbose", C.c_int),
         ("cuda_graphs", C.c_int), ("autotune", C.c_int),
+        ("propagate_vectors", C.c_int), ("share_frames", C.c_int),
     ]
 
 
@@ -68,7 +69,7 @@ class Stats(C.Structure):
     _fields_ = [
         ("kernel_launches", C.c_longlong), ("eig_sweeps", C.c_longlong), ("frame_steps", C.c_longlong),
         ("ms_build", C.c_double), ("ms_eig", C.c_double), ("ms_prop", C.c_double), ("ms_tcf", C.c_double),
-        ("ms_tridiag", C.c_double),
+        ("ms_tridiag", C.c_double), ("eig_matrices", C.c_longlong),
     ]
 
 

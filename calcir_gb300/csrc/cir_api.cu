@@ -21,6 +21,7 @@
 #include <cstring>
 #include <map>
 #include <tuple>
+#include <algorithm>
 #include <vector>
 
 namespace {
@@ -54,6 +55,7 @@ enum {
     B_FFT0, B_FFT1, B_FFTY, B_FFTX, B_PROF, B_DE, B_ERR, B_DC, B_TUNE,
     B_PSI, B_LAM, B_PA, B_PB, B_SEG, B_CKPT, B_R, B_T, B_GRAD,   // differentiation form
     B_VS, B_FS,                                    // split-BF16 propagation operands
+    B_UFR,                                         // run: distinct frames of a chunk and their multiplicity
     B_COUNT
 };
 
@@ -614,6 +616,9 @@ static std::vector<long long> step_key(const Group &g, int St, int K, int k0, in
             (long long)(uintptr_t)tcf, tile1, tile2, (long long)(uintptr_t)VS, (long long)(uintptr_t)FS};
 }
 
+static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long long sV, const float *w, long long sw,
+                         float dt, float *x, float *tmp, int &launches);
+
 // The frame-steps of one group: ntraj trajectories of one size, nsamples origins each.
 // dxyz / dbox hold all the group's frames on the device; fidx[(t*S + s)*K + k] is the frame
 // of step k of origin s of trajectory t.  res[t] receives trajectory t's results.
@@ -653,10 +658,14 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
     CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
     // the split-BF16 form propagates pre-split operands (k_tc_split.cu): per origin the
     // step's V as Vc and Vr and the transposed F and G, each a hi/lo pair of order ldh
-    const bool split = p.precision == CIR_PREC_BF16X3;
+    const bool vectors = p.propagate_vectors != 0;   // psi = F m(0) instead of F
+    const bool split = !vectors && p.precision == CIR_PREC_BF16X3;
     const int ldh = (int)cir_split_ld(n);
     const long long vs_el = (long long)n * ldh, fs_el = (long long)2 * n * ldh;   // elements per origin
-    if (split) {
+    if (vectors) {
+        CK(c->buf[B_PSI].ensure((size_t)St * n * CIR_PSI_LD * 4));
+        CK(c->buf[B_LAM].ensure((size_t)St * n * CIR_PSI_LD * 4));
+    } else if (split) {
         CK(c->buf[B_VS].ensure((size_t)4 * St * vs_el * 2));
         CK(c->buf[B_FS].ensure((size_t)4 * St * fs_el * 2));
     } else {
@@ -706,9 +715,45 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
     for (int k0 = 0; k0 < K; k0 += kn) {
         const int kc = std::min(kn, K - k0);
         const int nbc = St * kc;
+        // Matrix of origin s at step k0 + kk: base0 + kk + s * dlt.  Without sharing every
+        // origin has its own kc consecutive matrices (base0 = 0, dlt = kc).  With share_frames,
+        // when the chunk's frames lie on that pattern over their sorted distinct list (origins
+        // evenly spaced in one trajectory, as the reference places them), each distinct frame
+        // is built and diagonalised once and counts in the distributions as often as it is used.
+        int nmat = nbc, base0 = 0, dlt = kc;
+        int *ufr = nullptr;
+        if (p.share_frames && T == 1 && St > 1) {
+            std::vector<int> uf;
+            uf.reserve(nbc);
+            for (int s2 = 0; s2 < St; s2++)
+                for (int kk = 0; kk < kc; kk++) uf.push_back(fidx[(size_t)s2 * K + k0 + kk]);
+            std::sort(uf.begin(), uf.end());
+            uf.erase(std::unique(uf.begin(), uf.end()), uf.end());
+            auto pos = [&](int f) { return (int)(std::lower_bound(uf.begin(), uf.end(), f) - uf.begin()); };
+            const int b0 = pos(fidx[(size_t)k0]), d = pos(fidx[(size_t)K + k0]) - b0;
+            bool ok = (int)uf.size() < nbc && d > 0;
+            for (int s2 = 0; ok && s2 < St; s2++)
+                for (int kk = 0; ok && kk < kc; kk++) ok = pos(fidx[(size_t)s2 * K + k0 + kk]) == b0 + kk + s2 * d;
+            if (ok) {
+                nmat = (int)uf.size();
+                base0 = b0;
+                dlt = d;
+                std::vector<int> wgt(nmat, 0);
+                for (int s2 = 0; s2 < St; s2++)
+                    for (int kk = 0; kk < kc; kk++) wgt[b0 + kk + s2 * d]++;
+                CK(c->buf[B_UFR].ensure((size_t)nmat * 8));
+                ufr = c->buf[B_UFR].as<int>();
+                CK(cudaMemcpyAsync(ufr, uf.data(), (size_t)nmat * 4, cudaMemcpyHostToDevice, c->stream));
+                CK(cudaMemcpyAsync(ufr + nmat, wgt.data(), (size_t)nmat * 4, cudaMemcpyHostToDevice, c->stream));
+            }
+        }
         CK(cudaEventRecord(ev[1], c->stream));
-        k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(dxyz, dbox, c->buf[B_FIDX].as<int>(), g.natoms, St, kc, K,
-                                                             k0, c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
+        if (ufr)
+            k_gather_frames<<<dim3(8, nmat), 256, 0, c->stream>>>(dxyz, dbox, ufr, g.natoms, 1, nmat, nmat, 0,
+                                                                  c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
+        else
+            k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(dxyz, dbox, c->buf[B_FIDX].as<int>(), g.natoms, St, kc,
+                                                                 K, k0, c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
         CK(cudaGetLastError());
         launches++;
         BuildArgs a = build_args(c, g);
@@ -722,7 +767,7 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         a.ldv = ld;
         a.dip_fstride = 9LL * ld;
         a.pol_fstride = 9LL * ld;
-        CK(cir_launch_build(a, nbc, c->stream, &launches));
+        CK(cir_launch_build(a, nmat, c->stream, &launches));
         CK(cudaEventRecord(ev[2], c->stream));
         EighArgs e;
         memset(&e, 0, sizeof e);
@@ -741,7 +786,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         e.hist_ipr = c->buf[B_HIPR].as<double>();
         e.hist_mipr = c->buf[B_HMIPR].as<double>();
         e.out_of_range = c->buf[B_OOR].as<unsigned long long>();
-        e.hist_group = S * kc;        // the chunk's matrices of one trajectory share its histograms
+        e.hist_group = ufr ? 0 : S * kc;   // the chunk's matrices of one trajectory share its histograms
+        e.hist_weight = ufr ? ufr + nmat : nullptr;
         e.nomega = nomega;
         e.omegaStep = p.omegaStep;
         e.nchrom_mol = p.nchrom_mol;
@@ -753,26 +799,32 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         e.avef = p.avef;
         e.omegaStart = p.omegaStart;
         if (eigh_profiling()) {
-            CK(c->buf[B_PROF].ensure((size_t)nbc * CIR_EIG_PROF_SLOTS * 8));
-            CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nbc * CIR_EIG_PROF_SLOTS * 8, c->stream));
+            CK(c->buf[B_PROF].ensure((size_t)nmat * CIR_EIG_PROF_SLOTS * 8));
+            CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
             e.phase_ns = c->buf[B_PROF].as<unsigned long long>();
         }
-        CK(cir_launch_eigh(e, nbc, c->stream, &launches));
-        if (e.phase_ns) eigh_profile_report(e.phase_ns, nbc, c->stream);
+        CK(cir_launch_eigh(e, nmat, c->stream, &launches));
+        c->stats.eig_matrices += nmat;
+        if (e.phase_ns) eigh_profile_report(e.phase_ns, nmat, c->stream);
         CK(cudaEventRecord(ev[3], c->stream));
         if (k0 == 0) {
             // spectral density at step 0 of every origin (calcIR.cu:456-482), per trajectory
             for (int s = 0; s < St; s++) {
-                const size_t b = (size_t)s * kc;
+                const size_t b = (size_t)base0 + (size_t)s * dlt;
                 CK(cir_launch_spectral(A + b * mstride, ld, W + b * ld, M + b * 9 * ld, ld, n, c->buf[B_MU2].as<float>(),
                                        c->buf[B_SW].as<double>() + (size_t)(s / S) * nomega, nomega, p.omegaStart,
                                        p.omegaStep, p.t1, p.avef, c->stream, &launches));
             }
             // F = I and the t = 0 vectors (calcIR.cu:577-594)
-            if (split) CK(cir_launch_identity_t(Ft, n, ldh, fs_el, St, c->stream, &launches));
-            else CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, St, c->stream, &launches));
-            k_copy_m0<<<dim3(4, St), 256, 0, c->stream>>>(M, (long long)kc * 9 * ld, ld, M0);
-            CK(cudaGetLastError());
+            if (vectors) {
+                CK(cir_adj_psi_init(M + (size_t)base0 * 9 * ld, (long long)dlt * 9 * ld, ld, n, St,
+                                    c->buf[B_PSI].as<float>(), c->stream));
+            } else {
+                if (split) CK(cir_launch_identity_t(Ft, n, ldh, fs_el, St, c->stream, &launches));
+                else CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, St, c->stream, &launches));
+                k_copy_m0<<<dim3(4, St), 256, 0, c->stream>>>(M + (size_t)base0 * 9 * ld, (long long)dlt * 9 * ld, ld, M0);
+                CK(cudaGetLastError());
+            }
             launches++;
         }
         // the chunk's steps: F <- V_k exp(i L_k dt/hbar) V_k^T F for every origin
@@ -780,15 +832,28 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         auto run_steps = [&](int &nl) -> int {
             for (int k = k0; k < k0 + kc; k++) {
                 const int kk = k - k0;
+                const size_t mk = (size_t)base0 + kk;      // matrix of origin 0 at this step
+                if (vectors) {
+                    if (k > 0) {
+                        const int rc2 = psi_propagate(c, St, n, ld, A + mk * mstride, (long long)dlt * mstride, W + mk * ld,
+                                                      (long long)dlt * ld, p.dt, c->buf[B_PSI].as<float>(),
+                                                      c->buf[B_LAM].as<float>(), nl);
+                        if (rc2) return rc2;
+                    }
+                    CK(cir_adj_tcf(c->buf[B_PSI].as<float>(), M + mk * 9 * ld, (long long)dlt * 9 * ld, ld, n, St,
+                                   tcf + (size_t)k * 6, (long long)K * 6, c->stream));
+                    nl++;
+                    continue;
+                }
                 if (k > 0 && split) {
-                    CK(cir_launch_split_v(A + (size_t)kk * mstride, ld, (long long)kc * mstride, n, Vc, Vr, ldh, vs_el,
+                    CK(cir_launch_split_v(A + mk * mstride, ld, (long long)dlt * mstride, n, Vc, Vr, ldh, vs_el,
                                           St, c->stream, &nl));
                     SplitGemmArgs s1{};
                     s1.Ahi = Vc.hi; s1.Alo = Vc.lo; s1.lda = ldh; s1.sA = vs_el;       // V^T
                     s1.Bhi = Ft.hi; s1.Blo = Ft.lo; s1.ldb = ldh; s1.sB = fs_el;       // F
                     s1.Chi = Gt.hi; s1.Clo = Gt.lo; s1.ldc = ldh; s1.sC = fs_el;       // G, transposed
                     s1.M = n; s1.N = 2 * n; s1.K = n;
-                    s1.epilogue = 1; s1.w = W + (size_t)kk * ld; s1.wstride = kc * ld;
+                    s1.epilogue = 1; s1.w = W + mk * ld; s1.wstride = dlt * ld;
                     s1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
                     s1.err = c->buf[B_ERR].as<int>();
                     SplitGemmArgs s2 = s1;
@@ -799,8 +864,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                     CK(cir_launch_split_gemm(s1, St, c->stream, &nl));
                     CK(cir_launch_split_gemm(s2, St, c->stream, &nl));
                 } else if (k > 0) {
-                    int rc2 = propagate_dev(c, St, n, A + (size_t)kk * mstride, ld, (long long)kc * mstride,
-                                            W + (size_t)kk * ld, kc * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);
+                    int rc2 = propagate_dev(c, St, n, A + mk * mstride, ld, (long long)dlt * mstride,
+                                            W + mk * ld, dlt * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);
                     if (rc2) return rc2;
                 }
                 TcfArgs t;
@@ -809,8 +874,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                 t.sF = (long long)n * 2 * ld;
                 t.m0 = M0;
                 t.sm0 = 9LL * ld;
-                t.mt = M + (size_t)kk * 9 * ld;
-                t.smt = (long long)kc * 9 * ld;
+                t.mt = M + mk * 9 * ld;
+                t.smt = (long long)dlt * 9 * ld;
                 t.out = tcf + (size_t)k * 6;
                 t.sout = (long long)K * 6;
                 t.n = n;
@@ -826,7 +891,9 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
             return CIR_OK;
         };
         if (p.cuda_graphs) {
-            const std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2, vs, fs);
+            std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2, vs, fs);
+            key.insert(key.end(), {(long long)vectors, (long long)base0, (long long)dlt,
+                                   (long long)(uintptr_t)c->buf[B_PSI].p, (long long)(uintptr_t)c->buf[B_LAM].p});
             GraphEntry *ge = nullptr;
             for (auto &x : c->graphs)
                 if (x.key == key) ge = &x;
@@ -1090,8 +1157,9 @@ static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long 
     GemmArgs g2 = g1;
     g2.a_colmajor = true;                                              // V itself
     g2.B = tmp; g2.C = x; g2.epilogue = 0;
-    CK(cir_launch_gemm(g1, S, c->stream, &launches));
-    CK(cir_launch_gemm(g2, S, c->stream, &launches));
+    // n x 18 products: the 64 x 64 tiles give four times the blocks of the 128 x 128 ones
+    CK(cir_launch_gemm(g1, S, c->stream, &launches, CIR_GEMM_TILE_64));
+    CK(cir_launch_gemm(g2, S, c->stream, &launches, CIR_GEMM_TILE_64));
     return CIR_OK;
 }
 

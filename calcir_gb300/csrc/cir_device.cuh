@@ -72,6 +72,7 @@ struct EighArgs {
                           // set g uses hist_*[g*nomega ..] and out_of_range[g]
     unsigned long long *hist_count;
     double *hist_ipr, *hist_mipr;
+    const int *hist_weight;       // [nmat] times each matrix counts in the distributions (null: once)
     unsigned long long *out_of_range;
     int nomega, omegaStep, nchrom_mol;
     float avef, omegaStart;

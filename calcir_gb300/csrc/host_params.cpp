@@ -86,6 +86,8 @@ extern "C" int cir_params_default(cir_params *p) {
     p->verbose = 0;
     p->cuda_graphs = 1;
     p->autotune = 1;
+    p->propagate_vectors = 0;
+    p->share_frames = 0;
     return CIR_OK;
 }
 
@@ -163,6 +165,8 @@ extern "C" int cir_params_parse_file(const char *path, cir_params *p) {
         else if (!strcmp(k, "verbose")) scan_int(v, &p->verbose);
         else if (!strcmp(k, "cuda_graphs")) scan_int(v, &p->cuda_graphs);
         else if (!strcmp(k, "autotune")) scan_int(v, &p->autotune);
+        else if (!strcmp(k, "propagate_vectors")) scan_int(v, &p->propagate_vectors);
+        else if (!strcmp(k, "share_frames")) scan_int(v, &p->share_frames);
         else if (!strcmp(k, "precision")) {
             if (!strcmp(v, "fp32")) p->precision = CIR_PREC_FP32;
             else if (!strcmp(v, "tf32")) p->precision = CIR_PREC_TF32;

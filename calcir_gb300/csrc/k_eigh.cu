@@ -1156,12 +1156,13 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
                     const float wi = d[j] + a.avef;
                     const int bin = (int)roundf((wi - a.omegaStart) / (float)a.omegaStep);
                     const size_t grp = a.hist_group > 0 ? (size_t)(blockIdx.x / a.hist_group) : 0;
+                    const int wgt = a.hist_weight ? a.hist_weight[blockIdx.x] : 1;
                     if (bin >= 0 && bin < a.nomega) {
-                        atomicAdd(a.hist_count + grp * a.nomega + bin, 1ull);
-                        atomicAdd(a.hist_ipr + grp * a.nomega + bin, (double)(1.f / s4));
-                        atomicAdd(a.hist_mipr + grp * a.nomega + bin, (double)(1.f / m4));
+                        atomicAdd(a.hist_count + grp * a.nomega + bin, (unsigned long long)wgt);
+                        atomicAdd(a.hist_ipr + grp * a.nomega + bin, (double)wgt * (double)(1.f / s4));
+                        atomicAdd(a.hist_mipr + grp * a.nomega + bin, (double)wgt * (double)(1.f / m4));
                     } else {
-                        atomicAdd(a.out_of_range + grp, 1ull);
+                        atomicAdd(a.out_of_range + grp, (unsigned long long)wgt);
                     }
                 }
             }

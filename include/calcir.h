@@ -89,6 +89,11 @@ typedef struct cir_params {
     int   verbose;                 /* 0 silent, 1 reference-style progress on stdout   */
     int   cuda_graphs;             /* 1: replay the per-step launches from captured CUDA graphs */
     int   autotune;                /* 1: time the GEMM tile shapes once per problem shape      */
+    /* options of the run that give the same results by less work; off by default, so that
+       the default run does the reference's work (full F propagation, one eigensolve per
+       origin and step) */
+    int   propagate_vectors;       /* 1: propagate psi_a = F m_a(0) (9 complex vectors) instead of F */
+    int   share_frames;            /* 1: one eigensolve per distinct frame when origins overlap      */
 } cir_params;
 
 /* Whole-job results, caller-owned host arrays sized by cir_result_sizes. */
@@ -111,6 +116,7 @@ typedef struct cir_stats {
     long long frame_steps;              /* frame-steps processed by cir_run*              */
     double    ms_build, ms_eig, ms_prop, ms_tcf;   /* device time per stage of cir_run*  */
     double    ms_tridiag;               /* of ms_eig: the tridiagonalisation kernel       */
+    long long eig_matrices;             /* Hamiltonians built and diagonalised by cir_run* */
 } cir_stats;
 
 /* Parameters for the seeded synthetic water-box generator (replaces the .xtc source). */
