@@ -51,6 +51,12 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src, bool val
     const int sz = valid ? 4 : 0;   // 0: fill with zeros
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
 }
+// 16-byte asynchronous global-to-shared copy (zero fill when !valid)
+__device__ __forceinline__ void cp_async16(float *dst, const float *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int sz = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
@@ -73,7 +79,7 @@ __host__ __device__ constexpr int tb_stage(int nt) { return TB_KC * (2 * TB_ROWS
 __host__ __device__ inline size_t tq_union_floats(int n, int nt, bool blocked) {
     const size_t n4 = (size_t)((n + 3) & ~3), n32 = (size_t)((n + 31) & ~31);
     if (!blocked) return 4 * n4;
-    const size_t yw = n32 * (nt / 32), st = (size_t)tb_stage(nt);
+    const size_t yw = n32 * (nt / 32), st = 2 * (size_t)tb_stage(nt);   // two staging buffers
     return n32 + (yw > st ? yw : st) + 4 * TB_NB;
 }
 
@@ -398,7 +404,7 @@ __device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb
     const int R0 = q0 & ~3;
     const int mr = n - R0;
     const int ti = (mr + TB_ROWS - 1) / TB_ROWS, tj = (mr + BC - 1) / BC;
-    float *Vr = stage, *Wr = Vr + TB_KC * TB_ROWS, *Vc = Wr + TB_KC * TB_ROWS, *Wc = Vc + TB_KC * BC;
+    constexpr int TBS = tb_stage(NT);                 // floats of one staging buffer
     for (int I = 0; I < ti; I++) {
         const int jmax = min(tj - 1, (TB_ROWS * I + TB_ROWS - 1) / BC);
         for (int J = 0; J <= jmax; J++) {
@@ -416,9 +422,11 @@ __device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb
                     a[4 * hh + 0][j] = v.x; a[4 * hh + 1][j] = v.y; a[4 * hh + 2][j] = v.z; a[4 * hh + 3][j] = v.w;
                 }
             }
-            for (int j0 = 0; j0 < nb; j0 += TB_KC) {
+            // V and W rows of the tile's rows and columns, TB_KC panel columns at a time, copied
+            // by cp.async into one of two buffers while the other is in use
+            auto stage_chunk = [&](int j0, int buf) {
                 const int kc = min(TB_KC, nb - j0);
-                __syncthreads();   // the previous step's reads of the stage are done
+                float *Vr = stage + buf * TBS, *Wr = Vr + TB_KC * TB_ROWS, *Vc = Wr + TB_KC * TB_ROWS, *Wc = Vc + TB_KC * BC;
                 for (int idx = tid; idx < kc * F4; idx += NT) {
                     const int jj = idx / F4, o = idx - jj * F4;
                     int row, part;
@@ -428,15 +436,27 @@ __device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb
                     else { part = 3; row = cb + 4 * (o - TB_ROWS / 2 - BC / 4); }
                     const float *src = (part == 0 || part == 2) ? A + (size_t)(p0 + j0 + jj) * ld
                                                                 : Wb + (size_t)(j0 + jj) * ld;
-                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (row < n) v = *reinterpret_cast<const float4 *>(src + row);
                     float *dst = part == 0 ? Vr + jj * TB_ROWS + (row - rb)
                                : part == 1 ? Wr + jj * TB_ROWS + (row - rb)
                                : part == 2 ? Vc + jj * BC + (row - cb)
                                            : Wc + jj * BC + (row - cb);
-                    *reinterpret_cast<float4 *>(dst) = v;
+                    cp_async16(dst, row < n ? src + row : src, row < n);
                 }
-                __syncthreads();
+                cp_async_commit();
+            };
+            __syncthreads();   // the previous tile's reads of both buffers are done
+            stage_chunk(0, 0);
+            for (int j0 = 0, buf = 0; j0 < nb; j0 += TB_KC, buf ^= 1) {
+                const int kc = min(TB_KC, nb - j0);
+                if (j0 + TB_KC < nb) {
+                    stage_chunk(j0 + TB_KC, buf ^ 1);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+                __syncthreads();   // every thread's copies of this chunk are in
+                const float *Vr = stage + buf * TBS, *Wr = Vr + TB_KC * TB_ROWS, *Vc = Wr + TB_KC * TB_ROWS,
+                            *Wc = Vc + TB_KC * BC;
                 for (int jj = 0; jj < kc; jj++) {
                     const float4 v0 = *reinterpret_cast<const float4 *>(Vr + jj * TB_ROWS + 4 * tr);
                     const float4 v1 = *reinterpret_cast<const float4 *>(Vr + jj * TB_ROWS + 64 + 4 * tr);
@@ -453,6 +473,7 @@ __device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb
                         #pragma unroll
                         for (int j = 0; j < 4; j++) a[i][j] = fmaf(-vr[i], wc[j], fmaf(-wr[i], vc[j], a[i][j]));
                 }
+                __syncthreads();   // this buffer is refilled by the next chunk's copies
             }
             #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -568,7 +589,14 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
             for (int dq = warp; dq < 2 * kk; dq += NW) {
                 const float *col = dq < kk ? Wb + (size_t)dq * ld : A + (size_t)(p0 + dq - kk) * ld;
                 float s = 0.f;
-                for (int r = k + 1 + lane; r < n; r += 32) s += col[r] * x[r];
+                float s2 = 0.f;            // two chains, four loads in flight per lane
+                int r = k + 1 + lane;
+                for (; r + 32 < n; r += 64) {
+                    s = fmaf(col[r], x[r], s);
+                    s2 = fmaf(col[r + 32], x[r + 32], s2);
+                }
+                if (r < n) s = fmaf(col[r], x[r], s);
+                s += s2;
                 s = warp_sum(s);
                 if (lane == 0) {
                     if (dq < kk) t1[dq] = s;
@@ -644,7 +672,7 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     if constexpr (BLK) {
         // W of the current panel lives in Z, which phase 2 overwrites
         const int n32 = (n + 31) & ~31;
-        const int yws = max(n32 * NW, tb_stage(NT));
+        const int yws = max(n32 * NW, 2 * tb_stage(NT));
         tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red, pt);
     } else {
         float *vp = U, *wp = U + n4, *vc = U + 2 * n4, *wc = U + 3 * n4;
