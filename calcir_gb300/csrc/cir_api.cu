@@ -132,6 +132,16 @@ static void eigh_profile_report(const unsigned long long *dev, int nmat, cudaStr
                     "(chase %.3f incl. block search %.3f, apply %.3f, %.0f rotations in %.0f sweeps) sort %.3f\n",
             nmat, (t1 - t0) * 1e-6, tri / nmat * 1e-6, fq / nmat * 1e-6, qr / nmat * 1e-6, chase / nmat * 1e-6,
             search / nmat * 1e-6, apply / nmat * 1e-6, nrot / nmat, sweeps / nmat, srt / nmat * 1e-6);
+    double mp[5] = {0, 0, 0, 0, 0};
+    for (int m = 0; m < nmat; m++)
+        for (int q = 0; q < 5; q++) mp[q] += (double)h[(size_t)m * S + 7 + q];
+    double itn = 0, rts = 0;
+    for (int m = 0; m < nmat; m++) { itn += (double)h[(size_t)m * S + 18]; rts += (double)h[(size_t)m * S + 19]; }
+    if (rts > 0) fprintf(stderr, "eigh profile: secular equation: %.2f iterations per root over %.0f roots\n", itn / rts, rts);
+    if (mp[1] > 0)
+        fprintf(stderr, "eigh profile: merges, summed over a matrix's merges, mean per matrix (ms): setup and deflation "
+                        "%.3f roots %.3f z and norms %.3f ranking %.3f rotation %.3f\n",
+                mp[0] / nmat * 1e-6, mp[1] / nmat * 1e-6, mp[2] / nmat * 1e-6, mp[3] / nmat * 1e-6, mp[4] / nmat * 1e-6);
     if (tqp[0] + tqp[2] > 0)
         fprintf(stderr, "eigh profile: tridiagonalisation phases, mean per block (ms): column %.3f reflector %.3f "
                         "symv %.3f panel dots %.3f w %.3f trailing update %.3f\n",

@@ -49,7 +49,7 @@ struct BuildArgs {
     CirMaps maps;
 };
 
-constexpr int CIR_EIG_PROF_SLOTS = 18;
+constexpr int CIR_EIG_PROF_SLOTS = 20;
 
 struct EighArgs {
     float *A;             // [nmat] matrices, column j of matrix m at A + m*mstride + j*ld
@@ -79,8 +79,11 @@ struct EighArgs {
     // optional [nmat][CIR_EIG_PROF_SLOTS]: %globaltimer at the start and end of the
     // tridiagonalisation, of forming Q, of the QR iteration and of the ordering (0-6), then the
     // chase and apply times (ns), rotations, the chase's block-search time (ns) and sweeps
-    // (7-11), then the blocked tridiagonalisation's time (ns) in its column fetch, reflector,
-    // symmetric matrix-vector product, panel dot products, w and trailing update (12-17)
+    // (7-11; on the divide-and-conquer path: the merges' time in setup and deflation, secular
+    // roots, z and norms, ranking and rotation, summed over a matrix's merges), then the blocked
+    // tridiagonalisation's time (ns) in its column fetch, reflector, symmetric matrix-vector
+    // product, panel dot products, w and trailing update (12-17), then the secular equation's
+    // iterations and roots (18-19)
     unsigned long long *phase_ns;
 };
 

@@ -175,7 +175,8 @@ __device__ float dc_block_sum(float v, float *red) {
 }
 
 // root i of 1/rho + sum_j z2_j / (Dn_j - lambda); returns the origin index, *tau = lambda - Dn[origin]
-__device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rho, float z2sum, float *tau_out) {
+__device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rho, float z2sum, float *tau_out,
+                       int *iters) {
     const float rinv = 1.f / rho;
     int o;
     float lo, hi;
@@ -193,18 +194,25 @@ __device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rh
     const float dorg = Dn[o];
     const int ip = i < Kp - 1 ? i : Kp - 2;   // poles ip, ip+1 of the local model
     float t = 0.5f * (lo + hi);
-    for (int it = 0; it < 64; it++) {
-        float psi = 0.f, phi = 0.f, dpsi = 0.f, dphi = 0.f, di = 0.f, dj = 0.f;
-        for (int j = 0; j < Kp; j++) {
-            const float dl = (Dn[j] - dorg) - t;
-            const float rl = __frcp_rn(dl);   // one correctly rounded reciprocal per term
+    int it = 0;
+    for (; it < 64; it++) {
+        // the poles up to ip (psi) and beyond (phi) in two loops; one reciprocal per term,
+        // approximate (1 ulp), well inside the 8 eps sum(|terms|) convergence bound below
+        float psi = 0.f, phi = 0.f, dpsi = 0.f, dphi = 0.f;
+        for (int j = 0; j <= ip; j++) {
+            const float rl = __fdividef(1.f, (Dn[j] - dorg) - t);
             const float q = z2[j] * rl;
-            const float dq = q * rl;
-            if (j <= ip) { psi += q; dpsi += dq; }
-            else { phi += q; dphi += dq; }
-            if (j == ip) di = dl;
-            if (j == ip + 1) dj = dl;
+            psi += q;
+            dpsi = fmaf(q, rl, dpsi);
         }
+        for (int j = ip + 1; j < Kp; j++) {
+            const float rl = __fdividef(1.f, (Dn[j] - dorg) - t);
+            const float q = z2[j] * rl;
+            phi += q;
+            dphi = fmaf(q, rl, dphi);
+        }
+        const float di = ip >= 0 ? (Dn[ip] - dorg) - t : 0.f;
+        const float dj = ip + 1 < Kp ? (Dn[ip + 1] - dorg) - t : 0.f;
         const float g = rinv + psi + phi;
         const float errb = 8.f * (fabsf(psi) + fabsf(phi)) + 2.f * rinv;
         if (fabsf(g) <= DC_EPS * errb) break;
@@ -230,6 +238,7 @@ __device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rh
         if (done) break;
     }
     *tau_out = t;
+    *iters = it + 1;
     return o;
 }
 
@@ -245,6 +254,20 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
     int *org = reinterpret_cast<int *>(sm + L.org), *src = reinterpret_cast<int *>(sm + L.src);
     float *rot = sm + L.rot;
     __shared__ int s_kp, s_m, s_nd;
+    // optional per-phase timers of the merges (EighArgs.phase_ns slots 7-11, summed over merges)
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.y * CIR_EIG_PROF_SLOTS : nullptr;
+    unsigned long long tl = 0;
+    auto mark = [&](int slot) {
+        if (!pt) return;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (slot >= 0) atomicAdd(pt + slot, t - tl);
+            tl = t;
+        }
+    };
+    mark(-1);
     const int n = a.n, ld = a.ld, tid = threadIdx.x;
     const int mat = blockIdx.y, b = blockIdx.x;
     if (b >= (1 << level)) return;
@@ -295,11 +318,12 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
         for (int j = 0; j < K; j++) {
             if (rho * fabsf(zs[j]) <= tol) { kind[j] = -1; defl[nd++] = j; continue; }
             if (pj < 0) { pj = j; continue; }
-            float s = zs[pj], c = zs[j];
-            const float tt = hypotf(c, s), t = Ds[j] - Ds[pj];
-            c /= tt;
-            s = -s / tt;
-            if (fabsf(t * c * s) <= tol) {
+            // close pair test |t c s| <= tol with c = z_j / tt, s = -z_pj / tt, tt^2 = z_j^2 + z_pj^2,
+            // multiplied through by tt^2 (no division unless the pair deflates)
+            const float zj = zs[j], zp = zs[pj], t = Ds[j] - Ds[pj];
+            if (fabsf(t * zj * zp) <= tol * fmaf(zj, zj, zp * zp)) {
+                const float tt = hypotf(zj, zp);
+                const float c = zj / tt, s = -zp / tt;
                 zs[j] = tt;
                 zs[pj] = 0.f;
                 reinterpret_cast<int *>(rot)[4 * m] = pj;
@@ -337,13 +361,22 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
     }
     const float z2sum = dc_block_sum<NT>(zpart, red);
     __syncthreads();
+    mark(7);
     // secular roots
+    int nit = 0;
     for (int i = tid; i < Kp; i += NT) {
         float t;
-        org[i] = dc_root(i, Kp, Dn, z2, rho, z2sum, &t);
+        int itc;
+        org[i] = dc_root(i, Kp, Dn, z2, rho, z2sum, &t, &itc);
         tau[i] = t;
+        nit += itc;
+    }
+    if (pt && nit) {
+        atomicAdd(pt + 18, (unsigned long long)nit);
+        atomicAdd(pt + 19, (unsigned long long)((Kp - tid + NT - 1) / NT > 0 ? (Kp - tid + NT - 1) / NT : 0));
     }
     __syncthreads();
+    mark(8);
     // Gu-Eisenstat: zh_j^2 = -prod_i (Dn_j - lambda_i) / prod_{i != j} (Dn_j - Dn_i)
     for (int j = tid; j < Kp; j += NT) {
         const float dj = Dn[j];
@@ -359,11 +392,12 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
         const float base = Dn[org[i]], ti = tau[i];
         float sq = 0.f;
         for (int j = 0; j < Kp; j++) {
-            const float u = zh[j] / ((Dn[j] - base) - ti);
-            sq += u * u;
+            const float u = __fdividef(zh[j], (Dn[j] - base) - ti);
+            sq = fmaf(u, u, sq);
         }
         inv[i] = 1.f / sqrtf(sq);
     }
+    mark(9);
     // eigenvalues: roots then deflated values; ascending rank (ties by index)
     for (int q = tid; q < K; q += NT) vals[q] = q < Kp ? Dn[org[q]] + tau[q] : Ds[defl[q - Kp]];
     __syncthreads();
@@ -375,6 +409,7 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
         dw[a0 + r] = v;
     }
     __syncthreads();
+    mark(10);
     // M = G W in the sorted basis (row-major), then U = P M; without deflation rotations
     // (G = I) the columns go straight to U
     if (nrot == 0) {
@@ -391,6 +426,7 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
                 for (int r = 0; r < K; r++) U[(size_t)(a0 + perm[r]) * ld + a0 + c] = r == p ? 1.f : 0.f;
             }
         }
+        mark(11);
         return;
     }
     for (int c = tid; c < K; c += NT) {
