@@ -871,8 +871,13 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                     s2.Bhi = Gt.hi; s2.Blo = Gt.lo;
                     s2.Chi = Ft.hi; s2.Clo = Ft.lo;                                    // F', transposed
                     s2.epilogue = 0;
+                    // the step's correlation terms fused into F' = V G
+                    s2.tcf_m0 = M0; s2.tcf_sm0 = 9LL * ld;
+                    s2.tcf_mt = M + mk * 9 * ld; s2.tcf_smt = (long long)dlt * 9 * ld; s2.tcf_ldv = ld;
+                    s2.tcf_out = tcf + (size_t)k * 6; s2.tcf_sout = (long long)K * 6;
                     CK(cir_launch_split_gemm(s1, St, c->stream, &nl));
                     CK(cir_launch_split_gemm(s2, St, c->stream, &nl));
+                    continue;
                 } else if (k > 0) {
                     int rc2 = propagate_dev(c, St, n, A + mk * mstride, ld, (long long)dlt * mstride,
                                             W + mk * ld, dlt * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);

@@ -154,6 +154,15 @@ struct SplitGemmArgs {
     int wstride;
     float dt_over_hbar;
     int *err;
+    // fused correlation contraction for the propagation product F' = V G (out_mode 0): when
+    // tcf_out is set, row r of the product contracts with m(0) over the tile's complex columns
+    // and with m(k) at row r (the terms of k_tcf), and each block adds its six sums to
+    // tcf_out[batch * tcf_sout ..]
+    const float *tcf_m0, *tcf_mt;
+    long long tcf_sm0, tcf_smt;
+    int tcf_ldv;
+    double *tcf_out;
+    long long tcf_sout;
 };
 size_t cir_split_ld(int n);   // leading dimension of the split operands (n rounded up to 8)
 cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches);

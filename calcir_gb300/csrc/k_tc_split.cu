@@ -141,10 +141,15 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
     __syncwarp();
     ok = mbar_wait(done, 0) && ok;
     fence_after();
+    ok = __syncthreads_and(ok);   // one branch for the whole block (the epilogue reduces over it)
     if (!ok) {
         if (g.err && lane == 0) atomicExch(g.err, 1);
     } else {
         const int r = m0 + warp * 32 + lane;
+        const bool fuse = g.tcf_out != nullptr;
+        float pr[9], pi[9];
+        #pragma unroll
+        for (int a = 0; a < 9; a++) pr[a] = pi[a] = 0.f;
         float cph = 1.f, sph = 0.f;
         if (g.epilogue == 1 && r < g.M) {
             const float ph = g.w[(size_t)bz * g.wstride + r] * g.dt_over_hbar;
@@ -231,6 +236,56 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
                     for (int q = 0; q < 16; q++)
                         if (c + q < g.N) pf[q] = v[q];
                 }
+            }
+            if (fuse) {   // psi_a[r] += F'[r][q] m_a(0)[q] over the chunk's 8 complex columns
+                const float *m0p = g.tcf_m0 + (size_t)bz * g.tcf_sm0;
+                #pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int q = (c >> 1) + u;
+                    if (2 * q + 1 < g.N) {
+                        #pragma unroll
+                        for (int a = 0; a < 9; a++) {
+                            const float m = __ldg(m0p + (size_t)a * g.tcf_ldv + q);
+                            pr[a] = fmaf(v[2 * u], m, pr[a]);
+                            pi[a] = fmaf(v[2 * u + 1], m, pi[a]);
+                        }
+                    }
+                }
+            }
+        }
+        if (fuse) {
+            // the row's six terms (k_tcf's combination), then a block sum into the step's slot
+            __shared__ double tred[QT / 32][6];
+            float t6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (r < g.M) {
+                const float *mtp = g.tcf_mt + (size_t)bz * g.tcf_smt;
+                float cm[9];
+                #pragma unroll
+                for (int a = 0; a < 9; a++) cm[a] = mtp[(size_t)a * g.tcf_ldv + r];
+                const float ii_r = cm[3] * pr[3] + cm[4] * pr[4] + cm[5] * pr[5];
+                const float ii_i = cm[3] * pi[3] + cm[4] * pi[4] + cm[5] * pi[5];
+                const float ij_r = cm[6] * pr[6] + cm[7] * pr[7] + cm[8] * pr[8];
+                const float ij_i = cm[6] * pi[6] + cm[7] * pi[7] + cm[8] * pi[8];
+                const float jj_r = (cm[4] + cm[5]) * pr[3] + (cm[3] + cm[5]) * pr[4] + (cm[3] + cm[4]) * pr[5];
+                const float jj_i = (cm[4] + cm[5]) * pi[3] + (cm[3] + cm[5]) * pi[4] + (cm[3] + cm[4]) * pi[5];
+                t6[0] = cm[0] * pr[0] + cm[1] * pr[1] + cm[2] * pr[2];
+                t6[1] = cm[0] * pi[0] + cm[1] * pi[1] + cm[2] * pi[2];
+                t6[2] = (3.f * ii_r + jj_r + 4.f * ij_r) * (1.f / 15.f);
+                t6[3] = (3.f * ii_i + jj_i + 4.f * ij_i) * (1.f / 15.f);
+                t6[4] = (2.f * ii_r - jj_r + 6.f * ij_r) * (1.f / 30.f);
+                t6[5] = (2.f * ii_i - jj_i + 6.f * ij_i) * (1.f / 30.f);
+            }
+            #pragma unroll
+            for (int q = 0; q < 6; q++) {
+                const double d = warp_sum_d((double)t6[q]);
+                if (lane == 0) tred[warp][q] = d;
+            }
+            __syncthreads();
+            if (threadIdx.x < 6) {
+                double s = 0.0;
+                #pragma unroll
+                for (int w = 0; w < QT / 32; w++) s += tred[w][threadIdx.x];
+                atomicAdd(g.tcf_out + (size_t)bz * g.tcf_sout + threadIdx.x, s);
             }
         }
     }
