@@ -34,26 +34,25 @@ struct SplitMaps {
     CUtensorMap a_hi, a_lo, b_hi, b_lo;
 };
 
-constexpr int QM = 128, QN = 128;             // tile
+constexpr int QM = 128;                       // tile rows
 constexpr int QT = 128;                       // threads
-constexpr uint32_t Q_IDESC = make_idesc_mn(1u, QM, QN);   // BF16 operands
 
 // QK BF16 of K per stage = one swizzled row of 2 QK bytes (128-byte swizzle for QK = 64,
-// 64-byte for QK = 32), QS stages of A hi, A lo, B hi, B lo
-template <int QK, int QS> struct QCfg {
-    static constexpr int TILE = QM * QK * 2;
-    static constexpr int STAGE = 4 * TILE;
+// 64-byte for QK = 32), QS stages of A hi, A lo (QM rows) and B hi, B lo (QN rows)
+template <int QK, int QS, int QN> struct QCfg {
+    static constexpr int TILE_A = QM * QK * 2, TILE_B = QN * QK * 2;
+    static constexpr int STAGE = 2 * TILE_A + 2 * TILE_B;
     static constexpr size_t SMEM = (size_t)QS * STAGE + 1024 + 256;   // + alignment slack, barriers
-    static constexpr uint64_t LAYOUT = QK == 64 ? 2ull : 4ull;         // SWIZZLE_128B / SWIZZLE_64B
 };
 
 // shared-memory descriptor of a K-major tile in the swizzled layout a TMA box of QK BF16
 // x rows writes: 8-row atoms of 16 QK bytes (the stride byte offset), leading byte offset
-// unused (1), the layout type at bit 61
-template <int QK, int QS>
+// unused (1), the layout type at bit 61 (2: 128-byte swizzle, 4: 64-byte)
+template <int QK>
 __device__ __forceinline__ uint64_t desc_sw(uint32_t addr) {
+    constexpr uint64_t layout = QK == 64 ? 2ull : 4ull;
     return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((uint64_t)((16 * QK) >> 4) << 32) | (1ull << 46) |
-           (QCfg<QK, QS>::LAYOUT << 61);
+           (layout << 61);
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
@@ -71,9 +70,11 @@ __device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *map, 
 // One CTA per 128 x 128 tile of C.  Thread 0 is the TMA producer (stage s is refilled once
 // the MMAs that read it have committed to empty[s]), thread 32 issues the MMAs of a stage
 // once full[s] has received its bytes, and all four warps run the epilogue.
-template <int QK, int QS>
+template <int QK, int QS, int QN>
 __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMaps maps, SplitGemmArgs g) {
-    constexpr int Q_TILE = QCfg<QK, QS>::TILE, Q_STAGE = QCfg<QK, QS>::STAGE;
+    using C = QCfg<QK, QS, QN>;
+    constexpr int TA = C::TILE_A, TB = C::TILE_B, Q_STAGE = C::STAGE;
+    constexpr uint32_t Q_IDESC = make_idesc_mn(1u, QM, QN);   // BF16 operands
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
     const uint32_t sbase = (raw + 1023) & ~1023u;             // 1024-byte aligned stages
@@ -114,9 +115,9 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
             const uint32_t st = sbase + s * Q_STAGE;
             mbar_expect_tx(&full[s], Q_STAGE);
             tma_load3(st, &maps.a_hi, kt * QK, m0, bz, &full[s]);
-            tma_load3(st + Q_TILE, &maps.a_lo, kt * QK, m0, bz, &full[s]);
-            tma_load3(st + 2 * Q_TILE, &maps.b_hi, kt * QK, n0, bz, &full[s]);
-            tma_load3(st + 3 * Q_TILE, &maps.b_lo, kt * QK, n0, bz, &full[s]);
+            tma_load3(st + TA, &maps.a_lo, kt * QK, m0, bz, &full[s]);
+            tma_load3(st + 2 * TA, &maps.b_hi, kt * QK, n0, bz, &full[s]);
+            tma_load3(st + 2 * TA + TB, &maps.b_lo, kt * QK, n0, bz, &full[s]);
         }
     } else if (tid == 32) {
         for (int kt = 0; kt < KT && ok; kt++) {
@@ -128,8 +129,8 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
             #pragma unroll
             for (int ks = 0; ks < QK / 16; ks++) {
                 const uint32_t o = 32 * ks;                  // 16 BF16 of K inside the swizzled row
-                const uint64_t ah = desc_sw<QK, QS>(st + o), al = desc_sw<QK, QS>(st + Q_TILE + o);
-                const uint64_t bh = desc_sw<QK, QS>(st + 2 * Q_TILE + o), bl = desc_sw<QK, QS>(st + 3 * Q_TILE + o);
+                const uint64_t ah = desc_sw<QK>(st + o), al = desc_sw<QK>(st + TA + o);
+                const uint64_t bh = desc_sw<QK>(st + 2 * TA + o), bl = desc_sw<QK>(st + 2 * TA + TB + o);
                 mma_f16(tmem, ah, bh, Q_IDESC, (kt | ks) != 0);
                 mma_f16(tmem, ah, bl, Q_IDESC, 1u);
                 mma_f16(tmem, al, bh, Q_IDESC, 1u);
@@ -343,12 +344,13 @@ __global__ void k_identity_t(SplitMat F, int n, int ldh, long long sF) {
 
 size_t cir_split_ld(int n) { return (size_t)((n + 7) & ~7); }
 
-template <int QK, int QS>
-static cudaError_t launch_split(const SplitMaps &maps, const SplitGemmArgs &g, dim3 grid, cudaStream_t s) {
-    constexpr size_t smem = QCfg<QK, QS>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_tc_split<QK, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int QK, int QS, int QN>
+static cudaError_t launch_split(const SplitMaps &maps, const SplitGemmArgs &g, int batch, cudaStream_t s) {
+    constexpr size_t smem = QCfg<QK, QS, QN>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_tc_split<QK, QS, QN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_tc_split<QK, QS><<<grid, QT, smem, s>>>(maps, g);
+    dim3 grid((g.N + QN - 1) / QN, (g.M + QM - 1) / QM, batch);
+    k_tc_split<QK, QS, QN><<<grid, QT, smem, s>>>(maps, g);
     return cudaGetLastError();
 }
 
@@ -368,12 +370,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // Tensor map of one K-major BF16 operand: x = K (contiguous), y = rows (stride ld), z = matrix
 // (stride sb); boxes of 64 x 128 x 1 in the 128-byte swizzle, zero fill outside.
-static bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int K, int rows, int ld, long long sb, int batch, int QK) {
+static bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int K, int rows, int ld, long long sb, int batch, int QK,
+                     int box_rows) {
     auto fn = encode_fn();
     if (!fn) return false;
     const cuuint64_t dim[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)batch};
     const cuuint64_t stride[2] = {(cuuint64_t)ld * 2, (cuuint64_t)sb * 2};
-    const cuuint32_t box[3] = {(cuuint32_t)QK, QM, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)QK, (cuuint32_t)box_rows, 1};
     const cuuint32_t es[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dim, stride, box, es,
               CU_TENSOR_MAP_INTERLEAVE_NONE, QK == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
@@ -393,13 +396,17 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
                              // products of at most 4 K slices 2 stages (three CTAs per SM)
     SplitMaps maps;
     const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
-    if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK) ||
-        !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch, QK) ||
-        !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK) ||
-        !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK))
+    // wide products (the propagation, N = 2n >= 1024) in 128 x 256 tiles: a quarter less
+    // operand traffic per flop, two CTAs of 2 stages per SM (all 512 TMEM columns)
+    const int qn = (g.N >= 1024 && g.K > 4 * QK) ? 256 : 128;
+    if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK, QM) ||
+        !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch, QK, QM) ||
+        !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) ||
+        !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, qn))
         return cudaErrorInvalidValue;
-    dim3 grid((g.N + QN - 1) / QN, (g.M + QM - 1) / QM, batch);
-    const cudaError_t e = g.K <= 4 * QK ? launch_split<QK, 2>(maps, g, grid, s) : launch_split<QK, 3>(maps, g, grid, s);
+    const cudaError_t e = qn == 256 ? launch_split<QK, 2, 256>(maps, g, batch, s)
+                        : g.K <= 4 * QK ? launch_split<QK, 2, 128>(maps, g, batch, s)
+                                        : launch_split<QK, 3, 128>(maps, g, batch, s);
     if (e != cudaSuccess) return e;
     if (launches) *launches += 1;
     return cudaSuccess;
