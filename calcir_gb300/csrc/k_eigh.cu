@@ -526,24 +526,22 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
     const int nref = n - 2;       // columns 0 .. n-3 carry reflectors
     for (int p0 = 0; p0 < nref; p0 += TB_NB) {
         const int nb = min(TB_NB, nref - p0);
+        float xn2 = 0.f;   // |column k below k+1|^2; after the first column of a panel it comes
+                           // from the previous column's step (d), which also leaves d[k], the
+                           // alpha in red[48] and the rest of the column in x
         for (int kk = 0; kk < nb; kk++) {
             const int k = p0 + kk;
-            // (a) column k (rows k..n-1) with the panel's earlier updates applied
-            if (tid < kk) {
-                sv[tid] = A[(size_t)(p0 + tid) * ld + k];
-                sw[tid] = Wb[(size_t)tid * ld + k];
+            if (kk == 0) {
+                // (a) column k (rows k..n-1): the panel's first, unaffected by its reflectors
+                float part = 0.f;
+                for (int r = k + tid; r < n; r += NT) {
+                    const float v = A[(size_t)k * ld + r];
+                    if (r == k) d[k] = v;
+                    else if (r == k + 1) red[48] = v;
+                    else { x[r] = v; part += v * v; }
+                }
+                xn2 = block_sum<NT>(part, red);
             }
-            __syncthreads();
-            float part = 0.f;
-            for (int r = k + tid; r < n; r += NT) {
-                float v = A[(size_t)k * ld + r];
-                for (int jj = 0; jj < kk; jj++)
-                    v -= A[(size_t)(p0 + jj) * ld + r] * sw[jj] + Wb[(size_t)jj * ld + r] * sv[jj];
-                if (r == k) d[k] = v;
-                else if (r == k + 1) red[48] = v;
-                else { x[r] = v; part += v * v; }
-            }
-            const float xn2 = block_sum<NT>(part, red);
             mark(12);
             // (b) the reflector (slarfg convention: v[0] = 1, beta = -sign(alpha)*norm)
             if (tid == 0) {
@@ -605,30 +603,72 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
             }
             __syncthreads();
             mark(15);
-            // (d) w = tau (y - V t1 - W t2), then w -= (tau/2)(w.v) v, into column kk of Wb
-            float wr[RW];
+            // (d) w = tau (y - V t1 - W t2), then w -= (tau/2)(w.v) v, into column kk of Wb.
+            // When the next column is in this panel, the same pass over the panel's first kk
+            // columns also applies them to column k+1 (its step (a): rows k+1.., held by the
+            // threads that own those rows in step (b)), and the kk-th term v_k w_k[k+1] + w_k
+            // (v_k[k+1] = 1) follows once w is final.
+            const bool fuse = kk + 1 < nb;
+            if (fuse) {
+                if (tid < kk) {                     // row k+1 of the panel's V and W
+                    sv[tid] = A[(size_t)(p0 + tid) * ld + k + 1];
+                    sw[tid] = Wb[(size_t)tid * ld + k + 1];
+                }
+                __syncthreads();
+            }
+            float wr[RW], cr[RW];
             float dpart = 0.f;
             #pragma unroll
             for (int i = 0; i < RW; i++) {
                 const int r = k + 1 + tid + i * NT;
-                float w = 0.f;
+                float w = 0.f, c = 0.f;
                 if (r < n) {
                     float y = 0.f;
                     #pragma unroll
                     for (int ww = 0; ww < NW; ww++) y += ywall[(size_t)ww * n32 + r];
-                    for (int jj = 0; jj < kk; jj++)
-                        y -= A[(size_t)(p0 + jj) * ld + r] * t1[jj] + Wb[(size_t)jj * ld + r] * t2[jj];
+                    if (fuse) {
+                        c = A[(size_t)(k + 1) * ld + r];
+                        for (int jj = 0; jj < kk; jj++) {
+                            const float vj = A[(size_t)(p0 + jj) * ld + r], wj = Wb[(size_t)jj * ld + r];
+                            y -= vj * t1[jj] + wj * t2[jj];
+                            c -= vj * sw[jj] + wj * sv[jj];
+                        }
+                    } else {
+                        for (int jj = 0; jj < kk; jj++)
+                            y -= A[(size_t)(p0 + jj) * ld + r] * t1[jj] + Wb[(size_t)jj * ld + r] * t2[jj];
+                    }
                     w = tk * y;
                     dpart += w * x[r];
                 }
                 wr[i] = w;
+                cr[i] = c;
             }
             const float dot = block_sum<NT>(dpart, red);
             const float half = -0.5f * tk * dot;
             #pragma unroll
             for (int i = 0; i < RW; i++) {
                 const int r = k + 1 + tid + i * NT;
-                if (r < n) Wb[(size_t)kk * ld + r] = wr[i] + half * x[r];
+                if (r < n) {
+                    wr[i] += half * x[r];
+                    Wb[(size_t)kk * ld + r] = wr[i];
+                    if (r == k + 1) red[50] = wr[i];
+                }
+            }
+            if (fuse) {
+                __syncthreads();                   // w_k[k+1] in red[50]
+                const float wk1 = red[50];
+                float part = 0.f;
+                #pragma unroll
+                for (int i = 0; i < RW; i++) {
+                    const int r = k + 1 + tid + i * NT;
+                    if (r < n) {
+                        const float c = cr[i] - x[r] * wk1 - wr[i];
+                        if (r == k + 1) d[k + 1] = c;
+                        else if (r == k + 2) red[48] = c;
+                        else { x[r] = c; part += c * c; }
+                    }
+                }
+                xn2 = block_sum<NT>(part, red);
             }
             __syncthreads();
             mark(16);
