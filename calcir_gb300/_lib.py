@@ -43,7 +43,7 @@ class Params(C.Structure):
         ("synth_sigma_trans", C.c_float), ("synth_sigma_rot", C.c_float),
         ("precision", C.c_int), ("batch_frames", C.c_int), ("verbose", C.c_int),
         ("cuda_graphs", C.c_int), ("autotune", C.c_int),
-        ("propagate_vectors", C.c_int), ("share_frames", C.c_int),
+        ("propagate_vectors", C.c_int), ("share_frames", C.c_int), ("refine_eigen", C.c_int),
     ]
 
 

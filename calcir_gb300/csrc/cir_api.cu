@@ -56,6 +56,7 @@ enum {
     B_PSI, B_LAM, B_PA, B_PB, B_SEG, B_CKPT, B_R, B_T, B_GRAD,   // differentiation form
     B_VS, B_FS,                                    // split-BF16 propagation operands
     B_UFR,                                         // run: distinct frames of a chunk and their multiplicity
+    B_HREF, B_RW,                                  // FP64 eigenpair refinement: input copy, workspace
     B_COUNT
 };
 
@@ -171,6 +172,19 @@ static int stage_out(cir_ctx *c, void *dst, const void *dev, size_t bytes) {
     CK(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
     return CIR_OK;
 }
+
+// Compensated (Neumaier) FP64 sum: the running error term keeps what each addition rounds
+// away, so a long sum over time origins (hundreds of terms of either sign, partly
+// cancelling at long times) carries an error of O(eps) instead of O(S eps).
+struct CompSum {
+    double s = 0.0, e = 0.0;
+    void add(double x) {
+        const double t = s + x;
+        e += std::fabs(s) >= std::fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    double value() const { return s + e; }
+};
 
 static bool all_finite(const float *x, size_t n) {
     for (size_t i = 0; i < n; i++)
@@ -329,6 +343,8 @@ extern "C" int cir_build_hamiltonian(cir_ctx *c, int nframes, const float *xyz, 
     return CIR_OK;
 }
 
+static int setup_refine(cir_ctx *c, EighArgs &e, int nmat);
+
 extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     if (!c || !A || !w || nmat < 1 || n < 1) return cir_fail(CIR_ERR_ARG, "cir_eigh: bad argument");
     if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "cir_eigh: n = %d exceeds %d", n, cir_eigh_max_n());
@@ -365,6 +381,8 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
         CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
         a.phase_ns = c->buf[B_PROF].as<unsigned long long>();
     }
+    int rc;
+    if ((rc = setup_refine(c, a, nmat))) return rc;
     int launches = 0;
     CK(cir_launch_eigh(a, nmat, c->stream, &launches));
     count_launch(c, launches);
@@ -380,6 +398,24 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     c->stats.eig_sweeps += (long long)sweeps;
     for (int i = 0; i < nmat; i++)
         if (st[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached on matrix %d", i);
+    return CIR_OK;
+}
+
+// The optional FP64 refinement of the eigenpairs (refine_eigen steps): a copy of the nmat
+// input matrices at e.A, taken before the eigensolver overwrites them, and the workspace for
+// as many matrices at a time as fit in 2 GiB.
+static int setup_refine(cir_ctx *c, EighArgs &e, int nmat) {
+    if (c->p.refine_eigen <= 0) return CIR_OK;
+    const size_t mb = (size_t)e.mstride * 4;
+    CK(c->buf[B_HREF].ensure(nmat * mb));
+    CK(cudaMemcpyAsync(c->buf[B_HREF].p, e.A, nmat * mb, cudaMemcpyDeviceToDevice, c->stream));
+    const size_t per = cir_refine_bytes(e.n, e.ld);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nmat, ((size_t)2 << 30) / per));
+    CK(c->buf[B_RW].ensure(chunk * per));
+    e.Href = c->buf[B_HREF].as<float>();
+    e.RW = c->buf[B_RW].p;
+    e.refine_iters = c->p.refine_eigen;
+    e.refine_chunk = chunk;
     return CIR_OK;
 }
 
@@ -641,8 +677,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
     const long long steps = (long long)St * K;
 
     // chunk: kn consecutive steps of all St origins per batch
-    const size_t per_step = (size_t)2 * n * ld * 4 + cir_dc_bytes(n, ld) + cir_eigh_de_bytes(ld) +
-                            (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)g.natoms * 12 + 64;
+    const size_t per_step = (size_t)(p.refine_eigen > 0 ? 3 : 2) * n * ld * 4 + cir_dc_bytes(n, ld) +
+                            cir_eigh_de_bytes(ld) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)g.natoms * 12 + 64;
     size_t budget = (size_t)64 << 30;
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
@@ -813,6 +849,7 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
             CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
             e.phase_ns = c->buf[B_PROF].as<unsigned long long>();
         }
+        if ((rc = setup_refine(c, e, nmat))) return rc;
         CK(cir_launch_eigh(e, nmat, c->stream, &launches));
         c->stats.eig_matrices += nmat;
         if (e.phase_ns) eigh_profile_report(e.phase_ns, nmat, c->stream);
@@ -991,13 +1028,13 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         std::vector<double> damped[3];
         for (int q = 0; q < 3; q++) damped[q].assign((size_t)2 * K, 0.0);
         for (int k = 0; k < K; k++) {
-            double sum[6] = {0, 0, 0, 0, 0, 0};
+            CompSum sum[6];
             for (int s = tr * S; s < (tr + 1) * S; s++)
-                for (int q = 0; q < 6; q++) sum[q] += htcf[((size_t)s * K + k) * 6 + q];
+                for (int q = 0; q < 6; q++) sum[q].add(htcf[((size_t)s * K + k) * 6 + q]);
             const double dcy = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
             for (int q = 0; q < 3; q++) {
-                damped[q][2 * k] = sum[2 * q] * dcy;
-                damped[q][2 * k + 1] = sum[2 * q + 1] * dcy;
+                damped[q][2 * k] = sum[2 * q].value() * dcy;
+                damped[q][2 * k + 1] = sum[2 * q + 1].value() * dcy;
             }
         }
         double *outs[3] = {r->tcf_ir, r->tcf_vv, r->tcf_vh};
@@ -1312,11 +1349,13 @@ extern "C" int cir_loss_grad(cir_ctx *c, int nframes, const float *xyz, const fl
     for (int q = 0; q < 2; q++) X[q].assign((size_t)2 * K, 0.0);
     for (int k = 0; k < K; k++) {
         dcy[k] = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
+        CompSum sum[4];                              // IR (terms 0, 1) and VV (terms 2, 3)
         for (int s = 0; s < S; s++)
-            for (int q = 0; q < 2; q++) {           // IR (terms 0, 1) and VV (terms 2, 3)
-                X[q][2 * k] += htcf[((size_t)s * K + k) * 6 + 2 * q] * dcy[k];
-                X[q][2 * k + 1] += htcf[((size_t)s * K + k) * 6 + 2 * q + 1] * dcy[k];
-            }
+            for (int q = 0; q < 4; q++) sum[q].add(htcf[((size_t)s * K + k) * 6 + q]);
+        for (int q = 0; q < 2; q++) {
+            X[q][2 * k] = sum[2 * q].value() * dcy[k];
+            X[q][2 * k + 1] = sum[2 * q + 1].value() * dcy[k];
+        }
     }
     const int nfft = p.ntcfpoints + p.nzeros;
     const float *tg[2] = {target_ir, target_vv};

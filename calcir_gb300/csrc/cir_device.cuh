@@ -18,6 +18,20 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// Strict total order on (value, index) with NaN after every number: ranks counted with it
+// form a permutation whatever the values, so non-finite input can never turn a rank into an
+// out-of-range index.  cir_lt / cir_le are x < v and x <= v in the same order (no index).
+template <typename T>
+__device__ __forceinline__ bool cir_before(T a, int i, T b, int j) {
+    const bool na = a != a, nb = b != b;
+    if (na || nb) return na && nb ? i < j : nb;
+    return a < b || (a == b && i < j);
+}
+template <typename T>
+__device__ __forceinline__ bool cir_lt(T x, T v) { return x == x && (v != v || x < v); }
+template <typename T>
+__device__ __forceinline__ bool cir_le(T x, T v) { return v != v || (x == x && x <= v); }
+
 // Per-chromophore quantities produced by the field kernel, struct-of-arrays per frame:
 // row r of a frame's [CT_NROW][ld] block.
 enum {
@@ -85,6 +99,12 @@ struct EighArgs {
     // product, panel dot products, w and trailing update (12-17), then the secular equation's
     // iterations and roots (18-19)
     unsigned long long *phase_ns;
+    // optional FP64 refinement of the eigenpairs on the divide-and-conquer path (k_refine.cu),
+    // on when Href is not null: Href holds a copy of the input matrices (same strides as A), RW
+    // is scratch of cir_refine_bytes(n, ld) per matrix for refine_chunk matrices at a time
+    const float *Href;
+    void *RW;
+    int refine_iters, refine_chunk;
 };
 
 // kernel launchers (return cudaError_t of the launch)
@@ -99,6 +119,12 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
 // matrix), a.Z holds the blocks' T^T V^T.
 cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, float *U, int nmat, cudaStream_t s,
                                      int *launches);
+// FP64 refinement of eigenpairs (k_refine.cu): iters steps on the eigenvectors Z (row j =
+// eigenvector j, mstride / ld as A) of the matrices H (same strides) with eigenvalues w
+// (stride wstride), chunk matrices at a time in ws (cir_refine_bytes(n, ld) per matrix).
+size_t cir_refine_bytes(int n, int ld);
+cudaError_t cir_launch_refine(const float *H, float *Z, long long mstride, int ld, int n, float *w, long long wstride,
+                              int nmat, int iters, void *ws, int chunk, cudaStream_t s, int *launches);
 int cir_eigh_max_n();
 
 // batched SIMT FP32 GEMM, C = A * B (row-major B, C); A row- or column-major.

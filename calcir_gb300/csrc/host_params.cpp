@@ -88,6 +88,7 @@ extern "C" int cir_params_default(cir_params *p) {
     p->autotune = 1;
     p->propagate_vectors = 0;
     p->share_frames = 0;
+    p->refine_eigen = 0;
     return CIR_OK;
 }
 
@@ -167,6 +168,7 @@ extern "C" int cir_params_parse_file(const char *path, cir_params *p) {
         else if (!strcmp(k, "autotune")) scan_int(v, &p->autotune);
         else if (!strcmp(k, "propagate_vectors")) scan_int(v, &p->propagate_vectors);
         else if (!strcmp(k, "share_frames")) scan_int(v, &p->share_frames);
+        else if (!strcmp(k, "refine_eigen")) scan_int(v, &p->refine_eigen);
         else if (!strcmp(k, "precision")) {
             if (!strcmp(v, "fp32")) p->precision = CIR_PREC_FP32;
             else if (!strcmp(v, "tf32")) p->precision = CIR_PREC_TF32;
@@ -206,6 +208,8 @@ extern "C" int cir_params_finalize(cir_params *p) {
     if (cir_nomega(p) < 1) return cir_fail(CIR_ERR_ARG, "omegaStop must not be below omegaStart");
     if (p->precision < CIR_PREC_FP32 || p->precision > CIR_PREC_BF16X3)
         return cir_fail(CIR_ERR_ARG, "precision %d unknown", p->precision);
+    if (p->refine_eigen < 0 || p->refine_eigen > 8)
+        return cir_fail(CIR_ERR_ARG, "refine_eigen must be in [0, 8] (refinement steps)");
     return CIR_OK;
 }
 

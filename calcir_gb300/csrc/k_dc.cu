@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(128) k_dc_leaf(EighArgs a, int depth, float *Q
     // ascending order (ties by index)
     if (lane < s) {
         int r = 0;
-        for (int i = 0; i < s; i++) r += (d[i] < d[lane]) || (d[i] == d[lane] && i < lane);
+        for (int i = 0; i < s; i++) r += cir_before(d[i], i, d[lane], lane);
         rk[warp][lane] = r;
     }
     __syncwarp();
@@ -289,13 +289,14 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
     for (int i = tid; i < K; i += NT) {
         int rnk;
         const float v = D[i];
+        // (both halves ascend in the order of cir_before, NaN last, so the ranks are a permutation)
         if (i < k1) {   // number of D2 < v
             int lo = k1, hi = K;
-            while (lo < hi) { const int md = (lo + hi) >> 1; if (D[md] < v) lo = md + 1; else hi = md; }
+            while (lo < hi) { const int md = (lo + hi) >> 1; if (cir_lt(D[md], v)) lo = md + 1; else hi = md; }
             rnk = i + (lo - k1);
         } else {        // number of D1 <= v
             int lo = 0, hi = k1;
-            while (lo < hi) { const int md = (lo + hi) >> 1; if (D[md] <= v) lo = md + 1; else hi = md; }
+            while (lo < hi) { const int md = (lo + hi) >> 1; if (cir_le(D[md], v)) lo = md + 1; else hi = md; }
             rnk = (i - k1) + lo;
         }
         perm[rnk] = i;
@@ -404,7 +405,7 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
     for (int q = tid; q < K; q += NT) {
         const float v = vals[q];
         int r = 0;
-        for (int i = 0; i < K; i++) r += (vals[i] < v) || (vals[i] == v && i < q);
+        for (int i = 0; i < K; i++) r += cir_before(vals[i], i, v, q);
         src[r] = q;
         dw[a0 + r] = v;
     }
@@ -632,6 +633,13 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
     // with the free ping-pong buffer as scratch
     e = cir_launch_backtransform(a, buf[cur], buf[cur ^ 1], buf[2], nmat, s, &nl);
     if (e != cudaSuccess) return e;
+    // optional FP64 refinement of the eigenpairs (eigenvalues in DE row 0) before W and the
+    // distributions are written
+    if (a.Href) {
+        e = cir_launch_refine(a.Href, a.A, a.mstride, ld, n, a.DE, 3LL * ld, nmat, a.refine_iters, a.RW,
+                              a.refine_chunk, s, &nl);
+        if (e != cudaSuccess) return e;
+    }
     k_dc_finish<<<nmat, 256, 0, s>>>(a);
     nl += 1;
     if (launches) *launches += nl;

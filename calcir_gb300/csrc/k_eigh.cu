@@ -716,6 +716,10 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
         tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red, pt);
     } else {
         float *vp = U, *wp = U + n4, *vc = U + 2 * n4, *wc = U + 3 * n4;
+        // the first column reads vp / wp (scaled by zero) before any update has written them:
+        // clear them, since 0 * (a NaN or infinity left in shared memory) is NaN
+        for (int i = tid; i < 4 * n4; i += NT) U[i] = 0.f;
+        __syncthreads();
         bool pending = false;
         for (int k = 0; k + 2 < n; k++) {
             // (a) column k below the diagonal with the pending rank-2 update applied
@@ -1193,8 +1197,7 @@ __global__ void __launch_bounds__(NT, 3) k_eigh_qr(EighArgs a) {
             const float dj = d[j];
             int r = 0;
             for (int i = 0; i < n; i++) {
-                const float di = d[i];
-                r += (di < dj) || (di == dj && i < j);
+                r += cir_before(d[i], i, dj, j);
             }
             rank[j] = r;
             a.W[(size_t)blockIdx.x * a.wstride + r] = dj;

@@ -94,6 +94,10 @@ typedef struct cir_params {
        origin and step) */
     int   propagate_vectors;       /* 1: propagate psi_a = F m_a(0) (9 complex vectors) instead of F */
     int   share_frames;            /* 1: one eigensolve per distinct frame when origins overlap      */
+    /* precision option, off by default: steps of FP64 refinement of every eigendecomposition
+       (Rayleigh quotients, first-order eigenvector correction and re-orthogonalisation;
+       2 takes FP32 / split-BF16 eigenpairs to the accuracy of FP32 storage) */
+    int   refine_eigen;
 } cir_params;
 
 /* Whole-job results, caller-owned host arrays sized by cir_result_sizes. */

@@ -78,6 +78,21 @@ def test_finalize_rejects_what_the_reference_aborts_on(lib):
     assert (p.imodel, p.ispecies) == (1, 3)
 
 
+def test_engine_option_keys(lib, tmp_path):
+    """The engine's own keys (no counterpart in the reference) parse from input.inp, default
+    off, and refine_eigen (FP64 refinement steps) is range-checked."""
+    from calcir_gb300 import CirError, finalize
+    p = lib.default_params()
+    assert (p.propagate_vectors, p.share_frames, p.refine_eigen) == (0, 0, 0)
+    f = tmp_path / "input.inp"
+    f.write_text("species H2O\nmodel tip4p2005\nrefine_eigen 2\nshare_frames 1\npropagate_vectors 1\n")
+    p = finalize(lib.parse_input(str(f)))
+    assert (p.propagate_vectors, p.share_frames, p.refine_eigen) == (1, 1, 2)
+    for bad in (-1, 9):
+        with pytest.raises(CirError, match="refine_eigen"):
+            finalize(lib.default_params(species="H2O", refine_eigen=bad))
+
+
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_sizes_match_reference_outputs(lib, case):
     meta, gold = load_golden(case)
