@@ -289,23 +289,39 @@ def test_full_size_eigen_and_unitarity(lib, nmol):
     np.testing.assert_allclose(np.sum(dip[0].astype(np.float64) ** 2), np.sum(do ** 2), rtol=1e-4)
 
 
+_FULL_PRM = {"natom_mol": 4, "nchrom_mol": 2, "imodel": 1, "ispecies": 0, "map": 0, "ntcfpoints": 6,
+             "nsamples": 2, "sampleEvery": 0.03, "dt": 0.010, "t1": 0.260, "avef": 3415.0, "omegaStart": 1000,
+             "omegaStop": 5000, "omegaStep": 1, "nzeros": 2000, "beginTime": 0.0}
+_FULL_REF = {}
+
+
+def _full_case(lib, nmol):
+    """nmol molecules, 2 origins x 6 steps, and the oracle's whole job on them (computed once)."""
+    if nmol not in _FULL_REF:
+        prm = _FULL_PRM
+        xyz, box = lib.synth_trajectory(nmol, 10, seed=4)
+        fos = np.array([O.frame_index(prm, 0.010, s, k) for s in range(2) for k in range(6)], np.int32)
+        _FULL_REF[nmol] = (xyz, box, fos, O.run(prm, xyz, [box] * len(xyz), fos))
+    return _FULL_REF[nmol]
+
+
+@pytest.mark.parametrize("nmol", [512, 1024])
 @pytest.mark.parametrize("precision", ["fp32", "bf16x3", "tf32"])
-def test_run_full_size_against_oracle(lib, precision):
-    """512 molecules (the full configuration's system), 2 origins x 6 steps, vs the oracle:
-    the plain form within 1e-4 and the mixed forms (tensor-core propagation and eigenvector
-    products) within 1e-3 per spectrum."""
-    prm = {"natom_mol": 4, "nchrom_mol": 2, "imodel": 1, "ispecies": 0, "map": 0, "ntcfpoints": 6,
-           "nsamples": 2, "sampleEvery": 0.03, "dt": 0.010, "t1": 0.260, "avef": 3415.0, "omegaStart": 1000,
-           "omegaStop": 5000, "omegaStep": 1, "nzeros": 2000, "beginTime": 0.0}
-    xyz, box = lib.synth_trajectory(512, 10, seed=4)
-    fos = np.array([O.frame_index(prm, 0.010, s, k) for s in range(2) for k in range(6)], np.int32)
+def test_run_full_size_against_oracle(lib, precision, nmol):
+    """512 molecules (the full configuration's system, 1024 chromophores) and 1024 molecules
+    (2048 chromophores, the largest order of the eigensolver), 2 origins x 6 steps, vs the
+    oracle: the plain form within 1e-4 and the mixed forms (tensor-core propagation and
+    eigenvector products) within 1e-3 per spectrum."""
+    prm = _FULL_PRM
+    xyz, box, fos, ref = _full_case(lib, nmol)
     with lib.Engine(make_params(lib, prm, precision=precision), xyz.shape[1]) as eng:
         out = eng.run(xyz, box, fos)
-    ref = O.run(prm, xyz, [box] * len(xyz), fos)
-    _compare_run(out, ref, prm, SPEC_TOL if precision == "fp32" else MIXED_TOL, "full512-" + precision)
+    errs = {k: O.rel_l2(out[k], ref[k]) for k in ("tcf_ir", "tcf_vv", "tcf_vh", "sw", "ls_ir", "ls_vv", "ls_vh")}
+    print(f"{2 * nmol} chromophores {precision}:", {k: f"{v:.2e}" for k, v in errs.items()})
+    _compare_run(out, ref, prm, SPEC_TOL if precision == "fp32" else MIXED_TOL, f"full{nmol}-" + precision)
 
 
-@pytest.mark.parametrize("n", [200, 1024])
+@pytest.mark.parametrize("n", [200, 1024, 2048])
 def test_propagate_tensor_core_tf32(lib, n):
     """The tcgen05 TF32 propagation against the FP64 statement of the same step; TF32
     inputs carry 11 significant bits, so the bound is 2e-3 relative."""
@@ -321,11 +337,12 @@ def test_propagate_tensor_core_tf32(lib, n):
         ph = np.exp(1j * w[m].astype(np.float64) * np.float32(dt) / HBAR)
         ref = (V64 * ph[None, :]) @ (V64.T @ F[m].astype(np.complex128))
         err = O.rel_l2(out[m], ref)
+        print(f"tf32 propagation step, n={n}: relative L2 error {err:.2e}")
         assert err < 2e-3, err
         assert err > 1e-7, "tensor-core path produced FP32-exact output: is it running?"
 
 
-@pytest.mark.parametrize("n", [200, 1024])
+@pytest.mark.parametrize("n", [200, 1024, 2048])
 def test_propagate_tensor_core_bf16x3(lib, n):
     """3-pass split-BF16 tcgen05 propagation: about 16 significant bits per operand."""
     rng = np.random.default_rng(n + 11)
@@ -340,6 +357,7 @@ def test_propagate_tensor_core_bf16x3(lib, n):
         ph = np.exp(1j * w[m].astype(np.float64) * np.float32(dt) / HBAR)
         ref = (V64 * ph[None, :]) @ (V64.T @ F[m].astype(np.complex128))
         err = O.rel_l2(out[m], ref)
+        print(f"bf16x3 propagation step, n={n}: relative L2 error {err:.2e}")
         assert 1e-8 < err < 5e-5, err
 
 
