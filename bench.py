@@ -465,6 +465,21 @@ def main():
                               "ms_per_step": plain["ms"] / args.steps,
                               "stages_ms_per_step": {k: plain["stats"][k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
                               "mixed_over_plain": plain["ms"] / ms}
+    if rank == 0:
+        # FP32-SIMT / TF32 / FP64 cuBLAS peaks (not in the peak file), measured after the timed
+        # regions: the denominators of the plain form's SIMT propagation roofline
+        try:
+            from calcir_gb300 import peaks as peak_probe
+            extra = peak_probe.measure(quick=True)
+        except Exception as exc:        # a probe failure must not lose the bench line
+            extra = {"error": f"{type(exc).__name__}: {exc}"}
+        line["peaks_probe"] = extra
+        if plain is not None and "fp32_simt_tflops" in extra:
+            plain_prop = prop_flops / (plain["stats"]["ms_prop"] / args.steps * 1e-3) / 1e12
+            line["plain_fp32"]["roofline_propagation"] = {
+                "kernel": "k_sgemm (SIMT FP32 propagation GEMMs)", "bound": "fp32 simt", "achieved": plain_prop,
+                "peak": extra["fp32_simt_tflops"], "unit": "TFLOP/s", "frac": plain_prop / extra["fp32_simt_tflops"],
+                "peak_kind": "measured cuBLAS SGEMM, TF32 off (peaks_probe)"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rates, cores = cpu_port_rate(args.seed, args.cpu_sample, 2)
         line["cpu_baseline"] = {"value": float(np.mean(rates)), "unit": UNIT, "cores": cores, "kind": "port",

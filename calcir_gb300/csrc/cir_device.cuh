@@ -189,6 +189,7 @@ struct SplitGemmArgs {
     int tcf_ldv;
     double *tcf_out;
     long long tcf_sout;
+    int bz0;              // batch entry of blockIdx.z == 0 (set by the launcher when it splits a batch)
 };
 size_t cir_split_ld(int n);   // leading dimension of the split operands (n rounded up to 8)
 cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches);

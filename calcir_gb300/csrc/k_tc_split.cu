@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
     uint64_t *done = empty + QS;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int bz = blockIdx.z;
+    const int bz = blockIdx.z + g.bz0;
     const int m0 = blockIdx.y * QM, n0 = blockIdx.x * QN;
 
     if (warp == 0) {
@@ -354,6 +354,19 @@ static cudaError_t launch_split(const SplitMaps &maps, const SplitGemmArgs &g, i
     return cudaGetLastError();
 }
 
+// streaming multiprocessors of the current device (looked up once per device)
+static int sm_count() {
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 148;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 // cuTensorMapEncodeTiled from the driver, looked up once
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -404,6 +417,29 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
         !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) ||
         !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, qn))
         return cudaErrorInvalidValue;
+    if (qn == 256) {
+        // Wave quantisation: two 128 x 256 CTAs per SM.  When the last wave of the batch would
+        // hold less than half the slots, the batch entries that fill whole waves run in this
+        // shape and the rest in 128 x 64 tiles (four times the CTAs, a quarter of the work each,
+        // three per SM), so the tail costs about a quarter of a wave instead of a whole one.
+        const long long per = (long long)((g.N + 255) / 256) * ((g.M + QM - 1) / QM);
+        const long long slots = 2LL * sm_count();
+        const long long waves = per * batch / slots, rem = per * batch - waves * slots;
+        const int bmain = waves >= 1 ? (int)(waves * slots / per) : 0;
+        if (rem > 0 && 2 * rem < slots && bmain >= 1 && bmain < batch) {
+            SplitMaps tail = maps;
+            if (!make_map(&tail.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, 64) ||
+                !make_map(&tail.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, 64))
+                return cudaErrorInvalidValue;
+            cudaError_t e = launch_split<QK, 2, 256>(maps, g, bmain, s);
+            if (e != cudaSuccess) return e;
+            SplitGemmArgs gt = g;
+            gt.bz0 = g.bz0 + bmain;
+            if ((e = launch_split<QK, 3, 64>(tail, gt, batch - bmain, s)) != cudaSuccess) return e;
+            if (launches) *launches += 2;
+            return cudaSuccess;
+        }
+    }
     const cudaError_t e = qn == 256 ? launch_split<QK, 2, 256>(maps, g, batch, s)
                         : g.K <= 4 * QK ? launch_split<QK, 2, 128>(maps, g, batch, s)
                                         : launch_split<QK, 3, 128>(maps, g, batch, s);

@@ -321,6 +321,26 @@ def test_run_full_size_against_oracle(lib, precision, nmol):
     _compare_run(out, ref, prm, SPEC_TOL if precision == "fp32" else MIXED_TOL, f"full{nmol}-" + precision)
 
 
+def test_run_ten_origins_full_size(lib):
+    """Ten time origins of 1024 chromophores (the headline's origin count), 3 steps each: the
+    split-BF16 propagation runs each product as two whole waves of 128 x 256 tiles (nine
+    origins) and the tenth origin in 128 x 64 tiles.  Against the FP32 form of the same run
+    and the oracle; an error confined to the tail origin would still move the origin average
+    by a tenth of its size."""
+    prm = dict(_FULL_PRM, nsamples=10, ntcfpoints=3, sampleEvery=0.02)
+    fos = np.array([O.frame_index(prm, 0.010, s, k) for s in range(10) for k in range(3)], np.int32)
+    xyz, box = lib.synth_trajectory(512, int(fos.max()) + 1, seed=6)
+    outs = {}
+    for precision in ("fp32", "bf16x3"):
+        with lib.Engine(make_params(lib, prm, precision=precision), xyz.shape[1]) as eng:
+            outs[precision] = eng.run(xyz, box, fos)
+    ref = O.run(prm, xyz, [box] * len(xyz), fos)
+    for k in ("tcf_ir", "tcf_vv", "tcf_vh", "sw", "ls_ir", "ls_vv", "ls_vh"):
+        em, ep = O.rel_l2(outs["bf16x3"][k], ref[k]), O.rel_l2(outs["fp32"][k], ref[k])
+        print(f"ten origins {k}: bf16x3 {em:.2e}, fp32 {ep:.2e}")
+        assert ep < SPEC_TOL and em < 2e-4, (k, em, ep)
+
+
 @pytest.mark.parametrize("n", [200, 1024, 2048])
 def test_propagate_tensor_core_tf32(lib, n):
     """The tcgen05 TF32 propagation against the FP64 statement of the same step; TF32
