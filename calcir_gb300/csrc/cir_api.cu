@@ -1199,19 +1199,9 @@ static std::vector<int> lineshape_index(const cir_params *p, float *norm_out) {
 // row); FP32 SIMT GEMMs.  V: origin s at V + s*sV, w likewise; tmp: S x n x 18.
 static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long long sV, const float *w, long long sw,
                          float dt, float *x, float *tmp, int &launches) {
-    GemmArgs g1{};
-    g1.A = V; g1.lda = ld; g1.sA = sV; g1.a_colmajor = false;        // V^T (row-major view of V)
-    g1.B = x; g1.ldb = CIR_PSI_LD; g1.sB = (long long)n * CIR_PSI_LD;
-    g1.C = tmp; g1.ldc = CIR_PSI_LD; g1.sC = (long long)n * CIR_PSI_LD;
-    g1.M = n; g1.N = CIR_PSI_LD; g1.K = n;
-    g1.epilogue = 1; g1.w = w; g1.wstride = (int)sw;
-    g1.dt_over_hbar = (float)(dt / CIR_HBAR);
-    GemmArgs g2 = g1;
-    g2.a_colmajor = true;                                              // V itself
-    g2.B = tmp; g2.C = x; g2.epilogue = 0;
-    // n x 18 products: the 64 x 64 tiles give four times the blocks of the 128 x 128 ones
-    CK(cir_launch_gemm(g1, S, c->stream, &launches, CIR_GEMM_TILE_64));
-    CK(cir_launch_gemm(g2, S, c->stream, &launches, CIR_GEMM_TILE_64));
+    // X = e^{i L dt/hbar} V^T psi, then psi = V X: two streaming passes over V (k_adjoint.cu)
+    CK(cir_psi_step(V, ld, sV, n, w, sw, (float)(dt / CIR_HBAR), x, tmp, S, c->stream));
+    launches += 2;
     return CIR_OK;
 }
 

@@ -246,6 +246,9 @@ struct DthetaArgs {
     int n, ld, nchrom_mol, ispecies;
     double *out;          // [13] accumulated
 };
+// one step psi <- V e^{i L dt/hbar} V^T psi of S origins (psi, tmp: n x CIR_PSI_LD per origin)
+cudaError_t cir_psi_step(const float *V, int ld, long long sV, int n, const float *w, long long sw, float dt_over_hbar,
+                         float *psi, float *tmp, int S, cudaStream_t s);
 cudaError_t cir_adj_psi_init(const float *M, long long sM, int ld, int n, int S, float *psi, cudaStream_t s);
 cudaError_t cir_adj_tcf(const float *psi, const float *M, long long sM, int ld, int n, int S, double *out, long long sout,
                         cudaStream_t s);

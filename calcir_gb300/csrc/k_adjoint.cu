@@ -14,6 +14,8 @@
 // G_k and dL/dm(k) with the derivatives of the maps.
 #include "cir_device.cuh"
 
+#include <algorithm>
+
 namespace {
 
 constexpr int PSI_LD = CIR_PSI_LD;   // 9 complex columns
@@ -251,7 +253,141 @@ __global__ void __launch_bounds__(128) k_dtheta(DthetaArgs d) {
     }
 }
 
+// One propagation step of every origin's nine vectors, psi <- V e^{i L dt/hbar} V^T psi (the
+// F propagation of calcIR.cu:596-617 applied to psi = F m(0)), as two streaming passes over
+// the step's eigenvectors (row j of V = eigenvector j, stride ld, a multiple of 4):
+//   k_psi_rows: X[j][.] = e^{i w_j dt/hbar} sum_k V[j][k] psi[k][.]   (a warp per 4 rows j,
+//               16-byte loads along k against psi transposed in shared memory)
+//   k_psi_cols: psi[i][.] = sum_j V[j][i] X[j][.]   (32 columns i per block; its 8 warps take
+//               every 8th row j and add their partial sums in shared memory)
+// psi and X are n x 18 floats per origin (nine complex vectors, (re, im) pairs).
+constexpr int PSI_NT = 512;                  // threads of k_psi_rows (16 warps)
+constexpr int PSI_RW = 4;                    // rows per warp of k_psi_rows
+constexpr int PSI_ROWS = 16 * PSI_RW;        // rows of V per block of k_psi_rows
+constexpr int PSI_COLS = 32;                 // columns of V per block of k_psi_cols
+
+__host__ __device__ inline int psi_tld(int n) { return ((n + 3) & ~3) + 4; }   // row stride of psi^T
+
+__global__ void __launch_bounds__(PSI_NT) k_psi_rows(const float *V, int ld, long long sV, int n, const float *w,
+                                                     long long sw, float dtoh, const float *psi, float *X) {
+    extern __shared__ __align__(16) float pt[];       // psi^T: pt[q * tld + k], zero for k >= n
+    const int b = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tld = psi_tld(n);
+    const float *P = psi + (size_t)b * n * PSI_LD;
+    for (int t = threadIdx.x; t < n * PSI_LD; t += blockDim.x) {
+        const int k = t / PSI_LD, q = t - k * PSI_LD;
+        pt[q * tld + k] = P[t];
+    }
+    for (int t = threadIdx.x; t < PSI_LD * (tld - n); t += blockDim.x) {
+        const int q = t / (tld - n), k = n + t - q * (tld - n);
+        pt[q * tld + k] = 0.f;
+    }
+    __syncthreads();
+    const int j0 = blockIdx.x * PSI_ROWS + warp * PSI_RW;
+    if (j0 >= n) return;
+    const float *Vb = V + (size_t)b * sV;
+    float acc[PSI_RW][PSI_LD];
+    #pragma unroll
+    for (int r = 0; r < PSI_RW; r++)
+        #pragma unroll
+        for (int q = 0; q < PSI_LD; q++) acc[r][q] = 0.f;
+    const int n4 = (n + 3) >> 2;
+    for (int k4 = lane; k4 < n4; k4 += 32) {
+        const int k = 4 * k4;
+        float4 z[PSI_RW];
+        #pragma unroll
+        for (int r = 0; r < PSI_RW; r++) {
+            z[r] = j0 + r < n ? *reinterpret_cast<const float4 *>(Vb + (size_t)(j0 + r) * ld + k)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+            // the row's padding past n is not part of V: clear it (0 * a non-finite pad is NaN)
+            if (k + 1 >= n) z[r].y = 0.f;
+            if (k + 2 >= n) z[r].z = 0.f;
+            if (k + 3 >= n) z[r].w = 0.f;
+        }
+        #pragma unroll
+        for (int q = 0; q < PSI_LD; q++) {
+            const float4 p = *reinterpret_cast<const float4 *>(pt + q * tld + k);
+            #pragma unroll
+            for (int r = 0; r < PSI_RW; r++)
+                acc[r][q] = fmaf(z[r].x, p.x, fmaf(z[r].y, p.y, fmaf(z[r].z, p.z, fmaf(z[r].w, p.w, acc[r][q]))));
+        }
+    }
+    #pragma unroll
+    for (int r = 0; r < PSI_RW; r++)
+        #pragma unroll
+        for (int q = 0; q < PSI_LD; q++) acc[r][q] = warp_sum(acc[r][q]);
+    if (lane == 0) {
+        #pragma unroll
+        for (int r = 0; r < PSI_RW; r++) {
+            const int j = j0 + r;
+            if (j >= n) break;
+            float sn, cs;
+            sincosf(w[(size_t)b * sw + j] * dtoh, &sn, &cs);
+            float *x = X + ((size_t)b * n + j) * PSI_LD;
+            #pragma unroll
+            for (int q = 0; q < PSI_LD; q += 2) {   // (re, im) times exp(+i phase)
+                x[q] = cs * acc[r][q] - sn * acc[r][q + 1];
+                x[q + 1] = sn * acc[r][q] + cs * acc[r][q + 1];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_psi_cols(const float *V, int ld, long long sV, int n, const float *X,
+                                                  float *psi) {
+    extern __shared__ __align__(16) float xs[];       // X[j * 18 + q] (three blocks per SM at n = 1024),
+                                                      // then partial sums
+    const int b = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float *Xb = X + (size_t)b * n * PSI_LD;
+    for (int t = threadIdx.x; t < n * PSI_LD; t += blockDim.x) xs[t] = Xb[t];
+    __syncthreads();
+    const int i = blockIdx.x * PSI_COLS + lane;
+    float acc[PSI_LD];
+    #pragma unroll
+    for (int q = 0; q < PSI_LD; q++) acc[q] = 0.f;
+    if (i < n) {
+        const float *Vb = V + (size_t)b * sV + i;
+        #pragma unroll 4
+        for (int j = warp; j < n; j += 8) {
+            const float z = Vb[(size_t)j * ld];
+            const float2 *x2 = reinterpret_cast<const float2 *>(xs + j * PSI_LD);   // 8-byte aligned rows
+            #pragma unroll
+            for (int u = 0; u < PSI_LD / 2; u++) {
+                const float2 x = x2[u];
+                acc[2 * u] = fmaf(z, x.x, acc[2 * u]);
+                acc[2 * u + 1] = fmaf(z, x.y, acc[2 * u + 1]);
+            }
+        }
+    }
+    __syncthreads();                                  // xs is reused for the partial sums
+    float *part = xs + (warp * PSI_COLS + lane) * (PSI_LD + 1);
+    #pragma unroll
+    for (int q = 0; q < PSI_LD; q++) part[q] = acc[q];
+    __syncthreads();
+    for (int t = threadIdx.x; t < PSI_COLS * PSI_LD; t += blockDim.x) {
+        const int c = t / PSI_LD, q = t - c * PSI_LD, ic = blockIdx.x * PSI_COLS + c;
+        if (ic >= n) continue;
+        float sum = 0.f;
+        for (int wv = 0; wv < 8; wv++) sum += xs[(wv * PSI_COLS + c) * (PSI_LD + 1) + q];
+        psi[((size_t)b * n + ic) * PSI_LD + q] = sum;
+    }
+}
+
 }  // namespace
+
+cudaError_t cir_psi_step(const float *V, int ld, long long sV, int n, const float *w, long long sw, float dt_over_hbar,
+                         float *psi, float *tmp, int S, cudaStream_t s) {
+    if (n < 1 || S < 1 || S > 65535 || ld < n || (ld & 3) || (sV & 3) || (reinterpret_cast<uintptr_t>(V) & 15))
+        return cudaErrorInvalidValue;
+    const size_t smem_r = sizeof(float) * PSI_LD * (size_t)psi_tld(n);
+    const size_t smem_c = sizeof(float) * std::max((size_t)PSI_LD * n, (size_t)8 * PSI_COLS * (PSI_LD + 1));
+    cudaError_t e = cudaFuncSetAttribute(k_psi_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_psi_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c);
+    if (e != cudaSuccess) return e;
+    k_psi_rows<<<dim3((n + PSI_ROWS - 1) / PSI_ROWS, S), PSI_NT, smem_r, s>>>(V, ld, sV, n, w, sw, dt_over_hbar, psi,
+                                                                             tmp);
+    k_psi_cols<<<dim3((n + PSI_COLS - 1) / PSI_COLS, S), 256, smem_c, s>>>(V, ld, sV, n, tmp, psi);
+    return cudaGetLastError();
+}
 
 cudaError_t cir_adj_psi_init(const float *M, long long sM, int ld, int n, int S, float *psi, cudaStream_t s) {
     k_psi_init<<<dim3((n + 255) / 256, S), 256, 0, s>>>(M, sM, ld, n, psi);

@@ -4,6 +4,7 @@ CIR_EIGH_PROFILE=1 for the eigensolver's per-phase timers).
     python -m calcir_gb300.profile eigh --nmol 512 --batch 152
     python -m calcir_gb300.profile prop --n 1024 --nprop 10
     python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 250
+    python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 50 --propagate-vectors 1
 
 Every stage goes through the C ABI (libcalcir.so)."""
 from __future__ import annotations
@@ -40,9 +41,9 @@ def prop(n: int, nprop: int, precision: str = "fp32") -> None:
     print(f"prop N={n} x {nprop}: max |F| {np.abs(out).max():.4f}", flush=True)
 
 
-def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32") -> None:
+def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32", **options) -> None:
     p = cg.default_params(model="tip4p2005", species="H2O", ntcfpoints=ntcf, nsamples=nsamples, sampleEvery=2.0,
-                          avef=3415.0, omegaStart=1000, omegaStop=5000, omegaStep=1, precision=precision)
+                          avef=3415.0, omegaStart=1000, omegaStop=5000, omegaStep=1, precision=precision, **options)
     fos = cg.frame_table(p, 0.010)
     xyz, box = cg.synth_trajectory(nmol, int(fos.max()) + 1, seed=1)
     with cg.Engine(p, xyz.shape[1]) as eng:
@@ -65,13 +66,16 @@ def main() -> None:
     r.add_argument("--nsamples", type=int, default=10)
     r.add_argument("--ntcf", type=int, default=250)
     r.add_argument("--precision", default="fp32")
+    for opt in ("propagate-vectors", "share-frames", "refine-eigen"):
+        r.add_argument("--" + opt, type=int, default=0)
     a = ap.parse_args()
     if a.cmd == "eigh":
         eigh(a.nmol, [int(x) for x in a.batch.split(",")])
     elif a.cmd == "prop":
         prop(a.n, a.nprop, a.precision)
     else:
-        run(a.nmol, a.nsamples, a.ntcf, a.precision)
+        run(a.nmol, a.nsamples, a.ntcf, a.precision, propagate_vectors=a.propagate_vectors,
+            share_frames=a.share_frames, refine_eigen=a.refine_eigen)
 
 
 if __name__ == "__main__":
