@@ -44,6 +44,28 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def job_roofline(n, fps, pk, precision):
+    """The whole job against a time-weighted peak: W = 12.67 N^3 flops per frame-step (8 N^3
+    propagation, 2 N^3 back-transform, 4/3 N^3 tridiagonalisation, 4/3 N^3 divide and conquer);
+    in the mixed forms the propagation and back-transform on the tensor cores (BF16 peak / 3
+    passes for split-BF16), the rest at the FP32 SIMT rate; in the plain form everything at
+    the FP32 SIMT rate.  The SIMT rate is the nominal 152 SMs x 128 lanes x 2 flops x 2.07 GHz
+    (80.5 TFLOP/s); the measured SGEMM rate is in peaks_probe."""
+    simt = 152 * 128 * 2 * 2.07e9 / 1e12
+    w_tc, w_simt = 10.0, 8.0 / 3.0
+    if precision == "fp32":
+        peak = simt
+    else:
+        tc = pk["bf16_tflops"] / (3.0 if precision == "bf16x3" else 2.0)
+        peak = (w_tc + w_simt) / (w_tc / tc + w_simt / simt)
+    achieved = 12.67 * n ** 3 * fps / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "work": "12.67 N^3 flops per frame-step (propagation 8, back-transform 2, tridiagonalisation 4/3, "
+                    "divide and conquer 4/3)",
+            "peak_kind": "time-weighted: tensor share at the measured BF16 peak / passes (TF32 at half the BF16 "
+                         "rate), the rest at the nominal FP32 SIMT rate"}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -454,6 +476,7 @@ def main():
                                  "work": f"{8 * passes} N^3 tensor-pipe flops per origin-step ({passes} pass(es) of "
                                          "the two real N x 2N x N GEMMs, 8 N^3 algorithmic), 10 origins x 249 steps; "
                                          "time includes the V split and the correlation contraction"},
+        "roofline_job": job_roofline(n, value, pk, args.precision),
         "clocks": clk,
     }
     if options:

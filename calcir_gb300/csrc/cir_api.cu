@@ -349,6 +349,8 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     if (!c || !A || !w || nmat < 1 || n < 1) return cir_fail(CIR_ERR_ARG, "cir_eigh: bad argument");
     if (n > cir_eigh_max_n()) return cir_fail(CIR_ERR_ARG, "cir_eigh: n = %d exceeds %d", n, cir_eigh_max_n());
     if (nmat > 65535) return cir_fail(CIR_ERR_ARG, "cir_eigh: %d matrices in one call (at most 65535)", nmat);
+    if (!is_device_ptr(A) && !all_finite(A, (size_t)nmat * n * n))
+        return cir_fail(CIR_ERR_NONFINITE, "cir_eigh: the matrices contain NaN or Inf");
     // the kernel wants a leading dimension that is a multiple of 4: stage through a padded copy
     const int ld = (n + 3) & ~3;
     const size_t mb = (size_t)n * ld * 4;

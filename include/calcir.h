@@ -40,7 +40,7 @@ extern "C" {
 #define CIR_ERR_IO         -5   /* file could not be opened, read or written            */
 #define CIR_ERR_PARSE      -6   /* unknown model / species / map in the input           */
 #define CIR_ERR_STATE      -7   /* call out of order                                    */
-#define CIR_ERR_NONFINITE  -8   /* NaN or Inf in the positions or box                    */
+#define CIR_ERR_NONFINITE  -8   /* NaN or Inf in the positions, box or (host) matrices   */
 #define CIR_ERR_NODEVICE   -9   /* no CUDA device could be used                          */
 
 /* arithmetic of the propagation and correlation GEMMs */
