@@ -26,6 +26,9 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <mutex>
 
 namespace {
@@ -157,8 +160,27 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
             sincosf(ph, &sph, &cph);
         }
         __nv_bfloat16 *Ch = g.Chi + (size_t)bz * g.sC, *Cl = g.Clo + (size_t)bz * g.sC;
+        // epilogue 2 loads its row's D chunk one chunk ahead (16 values of hi and lo as four
+        // 16-byte words), so that the load's latency overlaps the previous chunk's work
+        const bool dpre = g.epilogue == 2 && r < g.M;
+        auto dload = [&](int cc, uint4 *d) -> bool {
+            const int c = n0 + cc;
+            const __nv_bfloat16 *dh = g.Dhi + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+            const __nv_bfloat16 *dl = g.Dlo + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+            if (c + 15 >= g.N || ((reinterpret_cast<uintptr_t>(dh) | reinterpret_cast<uintptr_t>(dl)) & 15)) return false;
+            d[0] = *reinterpret_cast<const uint4 *>(dh);
+            d[1] = *reinterpret_cast<const uint4 *>(dh + 8);
+            d[2] = *reinterpret_cast<const uint4 *>(dl);
+            d[3] = *reinterpret_cast<const uint4 *>(dl + 8);
+            return true;
+        };
+        uint4 dnext[4];
+        bool dnext_ok = dpre && dload(0, dnext);
         #pragma unroll 1
         for (int c0 = 0; c0 < QN; c0 += 16) {
+            uint4 dcur[4] = {dnext[0], dnext[1], dnext[2], dnext[3]};
+            const bool dcur_ok = dnext_ok;
+            if (dpre && c0 + 16 < QN) dnext_ok = dload(c0 + 16, dnext);
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
             if (r >= g.M) continue;
@@ -174,11 +196,10 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
             if (g.epilogue == 2) {   // C = D - A B, D a row-major split pair
                 const __nv_bfloat16 *dh = g.Dhi + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
                 const __nv_bfloat16 *dl = g.Dlo + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
-                if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(dh) | reinterpret_cast<uintptr_t>(dl)) & 15) == 0) {
+                if (dcur_ok) {
                     #pragma unroll
                     for (int h = 0; h < 2; h++) {
-                        const uint4 a = *reinterpret_cast<const uint4 *>(dh + 8 * h);
-                        const uint4 b = *reinterpret_cast<const uint4 *>(dl + 8 * h);
+                        const uint4 a = dcur[h], b = dcur[2 + h];
                         const uint32_t wa[4] = {a.x, a.y, a.z, a.w}, wb[4] = {b.x, b.y, b.z, b.w};
                         #pragma unroll
                         for (int u = 0; u < 8; u++) {
@@ -298,6 +319,227 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
     }
 }
 
+// Persistent, warp-specialised form of the same product for the propagation (epilogue 0 or
+// 1, transposed pair output, the fused correlation terms optional): one CTA per SM walks
+// the tiles t = blockIdx.x, + gridDim.x, ... (column tile fastest, then row tile, then
+// matrix).  Warp 0 lane 0 streams every tile's K slices through one QS-stage ring; warp 1
+// lane 0 issues the MMAs of tile i into tensor-memory accumulator i & 1 and commits it to
+// tfull; warps 2..5 (TMEM lane quarters 2, 3, 0, 1) drain accumulator i & 1 while tile
+// i + 1 is loaded and multiplied, then release it on tempty.  Every wait is bounded: a
+// timeout raises the CTA's abort flag and the error flag, every role leaves its loop, the
+// producer waits for its copies in flight, and the accumulators are freed.
+constexpr int PT = 192;                       // threads: producer, MMA, four epilogue warps
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+template <int QK, int QS, int QN>
+__global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ SplitMaps maps, SplitGemmArgs g,
+                                                      int tiles_n, int tiles_mn, int ntiles) {
+    using C = QCfg<QK, QS, QN>;
+    constexpr int TA = C::TILE_A, TB = C::TILE_B, Q_STAGE = C::STAGE;
+    constexpr uint32_t Q_IDESC = make_idesc_mn(1u, QM, QN);
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    const uint32_t sbase = (raw + 1023) & ~1023u;
+    unsigned char *smem = smem_raw + (sbase - raw);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + QS * Q_STAGE);   // [QS]
+    uint64_t *empty = full + QS;                                        // [QS]
+    uint64_t *tfull = empty + QS;                                       // [2]
+    uint64_t *tempty = tfull + 2;                                       // [2]
+    uint64_t *drain = tempty + 2;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                     "r"(2 * QN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < QS; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], 4);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    const int KT = (g.K + QK - 1) / QK;
+    auto fail = [&]() {
+        *abort_flag = 1;
+        if (g.err) atomicExch(g.err, 1);
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok && !*abort_flag; t += gridDim.x) {
+                const int bz = t / tiles_mn + g.bz0, rem = t % tiles_mn;
+                const int m0 = (rem / tiles_n) * QM, n0 = (rem % tiles_n) * QN;
+                for (int kt = 0; kt < KT; kt++, it++) {
+                    const int s = it % QS;
+                    if (it >= QS && !(ok = mbar_wait(&empty[s], ((it / QS) & 1) ^ 1))) break;
+                    if (*abort_flag) break;
+                    const uint32_t st = sbase + s * Q_STAGE;
+                    mbar_expect_tx(&full[s], Q_STAGE);
+                    tma_load3(st, &maps.a_hi, kt * QK, m0, bz, &full[s]);
+                    tma_load3(st + TA, &maps.a_lo, kt * QK, m0, bz, &full[s]);
+                    tma_load3(st + 2 * TA, &maps.b_hi, kt * QK, n0, bz, &full[s]);
+                    tma_load3(st + 2 * TA + TB, &maps.b_lo, kt * QK, n0, bz, &full[s]);
+                }
+            }
+            if (!ok) fail();
+            // the copies of the last QS slices may still be in flight: wait for them
+            for (uint32_t j = it > QS ? it - QS : 0; j < it; j++) mbar_wait(&full[j % QS], (j / QS) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true, issued = false;
+            int li = 0;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, li++) {
+                const int a = li & 1;
+                if (li >= 2 && !(ok = mbar_wait(&tempty[a], ((li >> 1) & 1) ^ 1))) break;
+                if (*abort_flag) break;
+                fence_after();
+                const uint32_t d = tmem + (uint32_t)(a * QN);
+                for (int kt = 0; kt < KT; kt++, it++) {
+                    const int s = it % QS;
+                    if (!(ok = mbar_wait(&full[s], (it / QS) & 1))) break;
+                    fence_after();
+                    const uint32_t st = sbase + s * Q_STAGE;
+                    #pragma unroll
+                    for (int ks = 0; ks < QK / 16; ks++) {
+                        const uint32_t o = 32 * ks;
+                        const uint64_t ah = desc_sw<QK>(st + o), al = desc_sw<QK>(st + TA + o);
+                        const uint64_t bh = desc_sw<QK>(st + 2 * TA + o), bl = desc_sw<QK>(st + 2 * TA + TB + o);
+                        mma_f16(d, ah, bh, Q_IDESC, (kt | ks) != 0);
+                        mma_f16(d, ah, bl, Q_IDESC, 1u);
+                        mma_f16(d, al, bh, Q_IDESC, 1u);
+                    }
+                    issued = true;
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                mma_commit(&tfull[a]);
+            }
+            if (!ok) fail();
+            if (issued) {   // every MMA issued has completed before the accumulators are freed
+                mma_commit(drain);
+                mbar_wait(drain, 0);
+            }
+        }
+    } else {
+        const int quarter = warp & 3, row = quarter * 32 + lane;
+        const bool fuse = g.tcf_out != nullptr;
+        int li = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
+            const int a = li & 1;
+            if (!mbar_wait(&tfull[a], (li >> 1) & 1)) {
+                fail();
+                break;
+            }
+            if (*abort_flag) break;
+            fence_after();
+            const int bz = t / tiles_mn + g.bz0, rem = t % tiles_mn;
+            const int m0 = (rem / tiles_n) * QM, n0 = (rem % tiles_n) * QN;
+            const int r = m0 + row;
+            float pr[9], pi[9];
+            #pragma unroll
+            for (int q = 0; q < 9; q++) pr[q] = pi[q] = 0.f;
+            float cph = 1.f, sph = 0.f;
+            if (g.epilogue == 1 && r < g.M) sincosf(g.w[(size_t)bz * g.wstride + r] * g.dt_over_hbar, &sph, &cph);
+            __nv_bfloat16 *Ch = g.Chi + (size_t)bz * g.sC, *Cl = g.Clo + (size_t)bz * g.sC;
+            const float *m0p = fuse ? g.tcf_m0 + (size_t)bz * g.tcf_sm0 : nullptr;
+            #pragma unroll 1
+            for (int c0 = 0; c0 < QN; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * QN + c0), v);
+                if (r >= g.M) continue;
+                if (g.epilogue == 1) {
+                    #pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const float re = v[q], im = v[q + 1];
+                        v[q] = cph * re - sph * im;
+                        v[q + 1] = sph * re + cph * im;
+                    }
+                }
+                const int c = n0 + c0;
+                #pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    if (c + q < g.N) {
+                        const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
+                        Ch[(size_t)(c + q) * g.ldc + r] = h;
+                        Cl[(size_t)(c + q) * g.ldc + r] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+                    }
+                }
+                if (fuse) {   // psi_a[r] += F'[r][q] m_a(0)[q] over the chunk's 8 complex columns
+                    #pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        const int q = (c >> 1) + u;
+                        if (2 * q + 1 < g.N) {
+                            #pragma unroll
+                            for (int b9 = 0; b9 < 9; b9++) {
+                                const float m = __ldg(m0p + (size_t)b9 * g.tcf_ldv + q);
+                                pr[b9] = fmaf(v[2 * u], m, pr[b9]);
+                                pi[b9] = fmaf(v[2 * u + 1], m, pi[b9]);
+                            }
+                        }
+                    }
+                }
+            }
+            // the accumulator is free for tile i + 2 once every lane has read it
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[a]);
+            if (fuse) {   // the row's six terms (k_tcf's combination); a warp sum per term, added in FP64
+                float t6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if (r < g.M) {
+                    const float *mtp = g.tcf_mt + (size_t)bz * g.tcf_smt;
+                    float cm[9];
+                    #pragma unroll
+                    for (int b9 = 0; b9 < 9; b9++) cm[b9] = mtp[(size_t)b9 * g.tcf_ldv + r];
+                    const float ii_r = cm[3] * pr[3] + cm[4] * pr[4] + cm[5] * pr[5];
+                    const float ii_i = cm[3] * pi[3] + cm[4] * pi[4] + cm[5] * pi[5];
+                    const float ij_r = cm[6] * pr[6] + cm[7] * pr[7] + cm[8] * pr[8];
+                    const float ij_i = cm[6] * pi[6] + cm[7] * pi[7] + cm[8] * pi[8];
+                    const float jj_r = (cm[4] + cm[5]) * pr[3] + (cm[3] + cm[5]) * pr[4] + (cm[3] + cm[4]) * pr[5];
+                    const float jj_i = (cm[4] + cm[5]) * pi[3] + (cm[3] + cm[5]) * pi[4] + (cm[3] + cm[4]) * pi[5];
+                    t6[0] = cm[0] * pr[0] + cm[1] * pr[1] + cm[2] * pr[2];
+                    t6[1] = cm[0] * pi[0] + cm[1] * pi[1] + cm[2] * pi[2];
+                    t6[2] = (3.f * ii_r + jj_r + 4.f * ij_r) * (1.f / 15.f);
+                    t6[3] = (3.f * ii_i + jj_i + 4.f * ij_i) * (1.f / 15.f);
+                    t6[4] = (2.f * ii_r - jj_r + 6.f * ij_r) * (1.f / 30.f);
+                    t6[5] = (2.f * ii_i - jj_i + 6.f * ij_i) * (1.f / 30.f);
+                }
+                #pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    const double dsum = warp_sum_d((double)t6[q]);
+                    if (lane == 0) atomicAdd(g.tcf_out + (size_t)bz * g.tcf_sout + q, dsum);
+                }
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * QN));
+    }
+}
+
 // Vc = V and Vr = V^T as BF16 hi/lo pairs; V column-major (V[k][i] at A[i*ld + k]).
 // 32 x 32 tiles through shared memory, block (32, 8).
 __global__ void k_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh, long long sV) {
@@ -367,6 +609,15 @@ static int sm_count() {
     return cache[dev];
 }
 
+// The persistent propagation kernel, unless CIR_SPLIT_PERSIST=0 (the one-tile-per-CTA kernel).
+static bool persist_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_SPLIT_PERSIST");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 // cuTensorMapEncodeTiled from the driver, looked up once
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -417,6 +668,24 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
         !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) ||
         !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, qn))
         return cudaErrorInvalidValue;
+    // the propagation products: persistent warp-specialised CTAs (one per SM), the epilogue
+    // of one tile overlapping the loads and MMAs of the next
+    if (qn == 256 && g.out_mode == 0 && (g.epilogue == 0 || g.epilogue == 1) && g.bz0 == 0 && persist_enabled()) {
+        constexpr int PQS = 4;
+        const int tiles_n = (g.N + 255) / 256, tiles_mn = tiles_n * ((g.M + QM - 1) / QM);
+        const long long ntl = (long long)tiles_mn * batch;
+        if (ntl <= INT32_MAX) {
+            constexpr size_t smem = QCfg<QK, PQS, 256>::SMEM;
+            cudaError_t e = cudaFuncSetAttribute(k_tc_persist<QK, PQS, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem);
+            if (e != cudaSuccess) return e;
+            const int grid = (int)std::min<long long>(ntl, sm_count());
+            k_tc_persist<QK, PQS, 256><<<grid, PT, smem, s>>>(maps, g, tiles_n, tiles_mn, (int)ntl);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if (launches) *launches += 1;
+            return cudaSuccess;
+        }
+    }
     if (qn == 256) {
         // Wave quantisation: two 128 x 256 CTAs per SM.  When the last wave of the batch would
         // hold less than half the slots, the batch entries that fill whole waves run in this
