@@ -324,11 +324,13 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
 // the tiles t = blockIdx.x, + gridDim.x, ... (column tile fastest, then row tile, then
 // matrix).  Warp 0 lane 0 streams every tile's K slices through one QS-stage ring; warp 1
 // lane 0 issues the MMAs of tile i into tensor-memory accumulator i & 1 and commits it to
-// tfull; warps 2..5 (TMEM lane quarters 2, 3, 0, 1) drain accumulator i & 1 while tile
-// i + 1 is loaded and multiplied, then release it on tempty.  Every wait is bounded: a
+// tfull; warps 2..9 drain accumulator i & 1 while tile i + 1 is loaded and multiplied
+// (warp w reads TMEM lane quarter w & 3, and the first or second half of the columns),
+// then release it on tempty.  Every wait is bounded: a
 // timeout raises the CTA's abort flag and the error flag, every role leaves its loop, the
 // producer waits for its copies in flight, and the accumulators are freed.
-constexpr int PT = 192;                       // threads: producer, MMA, four epilogue warps
+constexpr int PT = 320;                       // threads: producer, MMA, eight epilogue warps
+constexpr int PEW = 8;                        // epilogue warps
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
@@ -365,7 +367,7 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(&tfull[a], 1);
-            mbar_init(&tempty[a], 4);
+            mbar_init(&tempty[a], PEW);
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -443,6 +445,7 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
         }
     } else {
         const int quarter = warp & 3, row = quarter * 32 + lane;
+        const int cbeg = ((warp - 2) >> 2) * (QN / 2), cend = cbeg + QN / 2;   // this warp's columns
         const bool fuse = g.tcf_out != nullptr;
         int li = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
@@ -464,7 +467,7 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             __nv_bfloat16 *Ch = g.Chi + (size_t)bz * g.sC, *Cl = g.Clo + (size_t)bz * g.sC;
             const float *m0p = fuse ? g.tcf_m0 + (size_t)bz * g.tcf_sm0 : nullptr;
             #pragma unroll 1
-            for (int c0 = 0; c0 < QN; c0 += 16) {
+            for (int c0 = cbeg; c0 < cend; c0 += 16) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * QN + c0), v);
                 if (r >= g.M) continue;
@@ -486,16 +489,25 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                     }
                 }
                 if (fuse) {   // psi_a[r] += F'[r][q] m_a(0)[q] over the chunk's 8 complex columns
+                    const int q0 = c >> 1;
+                    const bool whole = 2 * (q0 + 8) <= g.N && (((uintptr_t)(m0p + q0) | ((size_t)g.tcf_ldv * 4)) & 15) == 0;
                     #pragma unroll
-                    for (int u = 0; u < 8; u++) {
-                        const int q = (c >> 1) + u;
-                        if (2 * q + 1 < g.N) {
+                    for (int b9 = 0; b9 < 9; b9++) {
+                        float m[8];
+                        if (whole) {   // the chunk's 8 values of m_a(0) as two 16-byte loads
+                            const float4 x = __ldg(reinterpret_cast<const float4 *>(m0p + (size_t)b9 * g.tcf_ldv + q0));
+                            const float4 y = __ldg(reinterpret_cast<const float4 *>(m0p + (size_t)b9 * g.tcf_ldv + q0 + 4));
+                            m[0] = x.x; m[1] = x.y; m[2] = x.z; m[3] = x.w;
+                            m[4] = y.x; m[5] = y.y; m[6] = y.z; m[7] = y.w;
+                        } else {
                             #pragma unroll
-                            for (int b9 = 0; b9 < 9; b9++) {
-                                const float m = __ldg(m0p + (size_t)b9 * g.tcf_ldv + q);
-                                pr[b9] = fmaf(v[2 * u], m, pr[b9]);
-                                pi[b9] = fmaf(v[2 * u + 1], m, pi[b9]);
-                            }
+                            for (int u = 0; u < 8; u++)
+                                m[u] = 2 * (q0 + u) + 1 < g.N ? __ldg(m0p + (size_t)b9 * g.tcf_ldv + q0 + u) : 0.f;
+                        }
+                        #pragma unroll
+                        for (int u = 0; u < 8; u++) {
+                            pr[b9] = fmaf(v[2 * u], m[u], pr[b9]);
+                            pi[b9] = fmaf(v[2 * u + 1], m[u], pi[b9]);
                         }
                     }
                 }
