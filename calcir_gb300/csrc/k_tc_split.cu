@@ -516,7 +516,8 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&tempty[a]);
-            if (fuse) {   // the row's six terms (k_tcf's combination); a warp sum per term, added in FP64
+            if (fuse) {   // the row's six terms (k_tcf's combination): a warp's 32 rows summed in FP32
+                          // (GB300's FP64 shuffles and adds would stall the epilogue), added in FP64
                 float t6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 if (r < g.M) {
                     const float *mtp = g.tcf_mt + (size_t)bz * g.tcf_smt;
@@ -538,8 +539,8 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                 }
                 #pragma unroll
                 for (int q = 0; q < 6; q++) {
-                    const double dsum = warp_sum_d((double)t6[q]);
-                    if (lane == 0) atomicAdd(g.tcf_out + (size_t)bz * g.tcf_sout + q, dsum);
+                    const float wsum = warp_sum(t6[q]);
+                    if (lane == 0) atomicAdd(g.tcf_out + (size_t)bz * g.tcf_sout + q, (double)wsum);
                 }
             }
         }
