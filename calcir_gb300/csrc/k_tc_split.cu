@@ -554,33 +554,40 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
 }
 
 // Vc = V and Vr = V^T as BF16 hi/lo pairs; V column-major (V[k][i] at A[i*ld + k]).
-// 32 x 32 tiles through shared memory, block (32, 8).
-__global__ void k_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh, long long sV) {
-    __shared__ float t[32][33];
+// 64 x 64 tiles through shared memory, block (32, 8): a thread reads two adjacent values
+// (8 bytes) and stores each output as a pair of BF16 (4 bytes); values past n are zero.
+__global__ void __launch_bounds__(256) k_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr,
+                                                 int ldh, long long sV) {
+    __shared__ float t[64][65];
     const int b = blockIdx.z;
-    const int i0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+    const int i0 = blockIdx.y * 64, k0 = blockIdx.x * 64;
     const float *a = A + (size_t)b * sA;
     const size_t ob = (size_t)b * sV;
-    for (int y = threadIdx.y; y < 32; y += 8) {
-        const int i = i0 + y, k = k0 + threadIdx.x;
-        float x = 0.f;
-        if (i < n && k < n) {
-            x = a[(size_t)i * ld + k];
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            Vc.hi[ob + (size_t)i * ldh + k] = h;
-            Vc.lo[ob + (size_t)i * ldh + k] = __float2bfloat16_rn(x - __bfloat162float(h));
+    auto store2 = [](__nv_bfloat16 *hi, __nv_bfloat16 *lo, float x0, float x1) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+        *reinterpret_cast<__nv_bfloat162 *>(hi) = h;
+        *reinterpret_cast<__nv_bfloat162 *>(lo) =
+            __floats2bfloat162_rn(x0 - __bfloat162float(h.x), x1 - __bfloat162float(h.y));
+    };
+    const int kx = k0 + 2 * threadIdx.x;
+    for (int y = threadIdx.y; y < 64; y += 8) {
+        const int i = i0 + y;
+        float2 x = make_float2(0.f, 0.f);
+        if (i < n && kx < n) {
+            x = *reinterpret_cast<const float2 *>(a + (size_t)i * ld + kx);   // ld and kx even
+            if (kx + 1 >= n) x.y = 0.f;
+            store2(Vc.hi + ob + (size_t)i * ldh + kx, Vc.lo + ob + (size_t)i * ldh + kx, x.x, x.y);
         }
-        t[y][threadIdx.x] = x;
+        t[y][2 * threadIdx.x] = x.x;
+        t[y][2 * threadIdx.x + 1] = x.y;
     }
     __syncthreads();
-    for (int y = threadIdx.y; y < 32; y += 8) {
-        const int k = k0 + y, i = i0 + threadIdx.x;     // Vr[k][i] = V[k][i] = A[i*ld + k]
-        if (i < n && k < n) {
-            const float x = t[threadIdx.x][y];
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            Vr.hi[ob + (size_t)k * ldh + i] = h;
-            Vr.lo[ob + (size_t)k * ldh + i] = __float2bfloat16_rn(x - __bfloat162float(h));
-        }
+    const int ix = i0 + 2 * threadIdx.x;
+    for (int y = threadIdx.y; y < 64; y += 8) {
+        const int k = k0 + y;                           // Vr[k][i] = V[k][i] = A[i*ld + k]
+        if (k < n && ix < n)
+            store2(Vr.hi + ob + (size_t)k * ldh + ix, Vr.lo + ob + (size_t)k * ldh + ix, t[2 * threadIdx.x][y],
+                   ix + 1 < n ? t[2 * threadIdx.x + 1][y] : 0.f);
     }
 }
 
@@ -732,7 +739,9 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
 
 cudaError_t cir_launch_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh,
                                long long sV, int batch, cudaStream_t s, int *launches) {
-    dim3 grid((n + 31) / 32, (n + 31) / 32, batch);
+    if ((ld & 1) || (ldh & 1) || (sA & 1) || (sV & 1) || (reinterpret_cast<uintptr_t>(A) & 7))
+        return cudaErrorInvalidValue;
+    dim3 grid((n + 63) / 64, (n + 63) / 64, batch);
     k_split_v<<<grid, dim3(32, 8), 0, s>>>(A, ld, sA, n, Vc, Vr, ldh, sV);
     if (launches) *launches += 1;
     return cudaGetLastError();
