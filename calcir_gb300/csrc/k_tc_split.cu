@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
     }
 }
 
-// Persistent, warp-specialised form of the same product for the propagation (epilogue 0 or
-// 1, transposed pair output, the fused correlation terms optional): one CTA per SM walks
+// Persistent, warp-specialised form of the same product (every epilogue and output form of
+// k_tc_split, the fused correlation terms optional): one CTA per SM walks
 // the tiles t = blockIdx.x, + gridDim.x, ... (column tile fastest, then row tile, then
 // matrix).  Warp 0 lane 0 streams every tile's K slices through one QS-stage ring; warp 1
 // lane 0 issues the MMAs of tile i into tensor-memory accumulator i & 1 and commits it to
@@ -466,8 +466,27 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             if (g.epilogue == 1 && r < g.M) sincosf(g.w[(size_t)bz * g.wstride + r] * g.dt_over_hbar, &sph, &cph);
             __nv_bfloat16 *Ch = g.Chi + (size_t)bz * g.sC, *Cl = g.Clo + (size_t)bz * g.sC;
             const float *m0p = fuse ? g.tcf_m0 + (size_t)bz * g.tcf_sm0 : nullptr;
+            // epilogue 2 loads its row's D chunk one chunk ahead (hi and lo as four 16-byte words)
+            const bool dpre = g.epilogue == 2 && r < g.M;
+            auto dload = [&](int cc, uint4 *dd) -> bool {
+                const int c = n0 + cc;
+                const __nv_bfloat16 *dh = g.Dhi + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                const __nv_bfloat16 *dl = g.Dlo + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                if (c + 15 >= g.N || ((reinterpret_cast<uintptr_t>(dh) | reinterpret_cast<uintptr_t>(dl)) & 15))
+                    return false;
+                dd[0] = *reinterpret_cast<const uint4 *>(dh);
+                dd[1] = *reinterpret_cast<const uint4 *>(dh + 8);
+                dd[2] = *reinterpret_cast<const uint4 *>(dl);
+                dd[3] = *reinterpret_cast<const uint4 *>(dl + 8);
+                return true;
+            };
+            uint4 dnext[4];
+            bool dnext_ok = dpre && dload(cbeg, dnext);
             #pragma unroll 1
             for (int c0 = cbeg; c0 < cend; c0 += 16) {
+                uint4 dcur[4] = {dnext[0], dnext[1], dnext[2], dnext[3]};
+                const bool dcur_ok = dnext_ok;
+                if (dpre && c0 + 16 < cend) dnext_ok = dload(c0 + 16, dnext);
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * QN + c0), v);
                 if (r >= g.M) continue;
@@ -480,12 +499,71 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                     }
                 }
                 const int c = n0 + c0;
-                #pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    if (c + q < g.N) {
-                        const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
-                        Ch[(size_t)(c + q) * g.ldc + r] = h;
-                        Cl[(size_t)(c + q) * g.ldc + r] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+                if (g.epilogue == 2) {   // C = D - A B, D a row-major split pair
+                    if (dcur_ok) {
+                        #pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const uint32_t wa[4] = {dcur[h].x, dcur[h].y, dcur[h].z, dcur[h].w};
+                            const uint32_t wb[4] = {dcur[2 + h].x, dcur[2 + h].y, dcur[2 + h].z, dcur[2 + h].w};
+                            #pragma unroll
+                            for (int u = 0; u < 8; u++) {
+                                const float xh = __uint_as_float((wa[u / 2] >> (16 * (u & 1))) << 16);
+                                const float xl = __uint_as_float((wb[u / 2] >> (16 * (u & 1))) << 16);
+                                v[8 * h + u] = (xh + xl) - v[8 * h + u];
+                            }
+                        }
+                    } else {
+                        const __nv_bfloat16 *dh = g.Dhi + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                        const __nv_bfloat16 *dl = g.Dlo + (size_t)bz * g.sD + (size_t)r * g.ldd + c;
+                        #pragma unroll
+                        for (int q = 0; q < 16; q++)
+                            v[q] = (c + q < g.N ? __bfloat162float(dh[q]) + __bfloat162float(dl[q]) : 0.f) - v[q];
+                    }
+                }
+                if (g.out_mode == 0) {           // transposed split pair
+                    #pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        if (c + q < g.N) {
+                            const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
+                            Ch[(size_t)(c + q) * g.ldc + r] = h;
+                            Cl[(size_t)(c + q) * g.ldc + r] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+                        }
+                    }
+                } else if (g.out_mode == 1) {    // row-major split pair
+                    uint32_t wh[8], wl[8];
+                    #pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const __nv_bfloat16 h0 = __float2bfloat16_rn(v[q]), h1 = __float2bfloat16_rn(v[q + 1]);
+                        const __nv_bfloat16 l0 = __float2bfloat16_rn(v[q] - __bfloat162float(h0));
+                        const __nv_bfloat16 l1 = __float2bfloat16_rn(v[q + 1] - __bfloat162float(h1));
+                        wh[q / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                        wl[q / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                    }
+                    __nv_bfloat16 *ph = Ch + (size_t)r * g.ldc + c, *pl = Cl + (size_t)r * g.ldc + c;
+                    if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(ph) | reinterpret_cast<uintptr_t>(pl)) & 15) == 0) {
+                        #pragma unroll
+                        for (int q = 0; q < 8; q += 4) {
+                            *reinterpret_cast<uint4 *>(ph + 2 * q) = make_uint4(wh[q], wh[q + 1], wh[q + 2], wh[q + 3]);
+                            *reinterpret_cast<uint4 *>(pl + 2 * q) = make_uint4(wl[q], wl[q + 1], wl[q + 2], wl[q + 3]);
+                        }
+                    } else {
+                        #pragma unroll
+                        for (int q = 0; q < 16; q++)
+                            if (c + q < g.N) {
+                                ph[q] = __ushort_as_bfloat16((unsigned short)(wh[q / 2] >> (16 * (q & 1))));
+                                pl[q] = __ushort_as_bfloat16((unsigned short)(wl[q / 2] >> (16 * (q & 1))));
+                            }
+                    }
+                } else {                         // row-major FP32
+                    float *pf = g.Cf + (size_t)bz * g.sC + (size_t)r * g.ldc + c;
+                    if (c + 15 < g.N && (reinterpret_cast<uintptr_t>(pf) & 15) == 0) {
+                        #pragma unroll
+                        for (int q = 0; q < 16; q += 4)
+                            *reinterpret_cast<float4 *>(pf + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                    } else {
+                        #pragma unroll
+                        for (int q = 0; q < 16; q++)
+                            if (c + q < g.N) pf[q] = v[q];
                     }
                 }
                 if (fuse) {   // psi_a[r] += F'[r][q] m_a(0)[q] over the chunk's 8 complex columns
@@ -688,20 +766,23 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
         !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) ||
         !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, qn))
         return cudaErrorInvalidValue;
-    // the propagation products: persistent warp-specialised CTAs (one per SM), the epilogue
-    // of one tile overlapping the loads and MMAs of the next
-    if (qn == 256 && g.out_mode == 0 && (g.epilogue == 0 || g.epilogue == 1) && g.bz0 == 0 && persist_enabled()) {
-        constexpr int PQS = 4;
-        const int tiles_n = (g.N + 255) / 256, tiles_mn = tiles_n * ((g.M + QM - 1) / QM);
+    // persistent warp-specialised CTAs (one per SM), the epilogue of one tile overlapping the
+    // loads and MMAs of the next: 128 x 256 tiles in a 4-stage ring for the propagation,
+    // 128 x 128 tiles in a 6-stage ring otherwise
+    if (g.bz0 == 0 && persist_enabled()) {
+        const int tiles_n = (g.N + qn - 1) / qn, tiles_mn = tiles_n * ((g.M + QM - 1) / QM);
         const long long ntl = (long long)tiles_mn * batch;
         if (ntl <= INT32_MAX) {
-            constexpr size_t smem = QCfg<QK, PQS, 256>::SMEM;
-            cudaError_t e = cudaFuncSetAttribute(k_tc_persist<QK, PQS, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem);
-            if (e != cudaSuccess) return e;
             const int grid = (int)std::min<long long>(ntl, sm_count());
-            k_tc_persist<QK, PQS, 256><<<grid, PT, smem, s>>>(maps, g, tiles_n, tiles_mn, (int)ntl);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            auto go = [&](auto kern, size_t smem) -> cudaError_t {
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return e;
+                kern<<<grid, PT, smem, s>>>(maps, g, tiles_n, tiles_mn, (int)ntl);
+                return cudaGetLastError();
+            };
+            const cudaError_t e = qn == 256 ? go(k_tc_persist<QK, 4, 256>, QCfg<QK, 4, 256>::SMEM)
+                                            : go(k_tc_persist<QK, 6, 128>, QCfg<QK, 6, 128>::SMEM);
+            if (e != cudaSuccess) return e;
             if (launches) *launches += 1;
             return cudaSuccess;
         }
