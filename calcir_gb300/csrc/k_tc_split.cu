@@ -353,6 +353,10 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
     uint64_t *drain = tempty + 2;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tslot + 1);
+    // the fused contraction's per-tile sums: the epilogue warps of accumulator a add into
+    // tred[a], and the last of them adds the six totals to the step's slots in FP64
+    __shared__ double tred[2][6];
+    __shared__ int tcnt[2];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 1) {
@@ -371,6 +375,10 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
+        for (int a = 0; a < 2; a++) {
+            tcnt[a] = 0;
+            for (int q = 0; q < 6; q++) tred[a][q] = 0.0;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
@@ -590,10 +598,6 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                     }
                 }
             }
-            // the accumulator is free for tile i + 2 once every lane has read it
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[a]);
             if (fuse) {   // the row's six terms (k_tcf's combination): a warp's 32 rows summed in FP32
                           // (GB300's FP64 shuffles and adds would stall the epilogue), added in FP64
                 float t6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -615,12 +619,30 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                     t6[4] = (2.f * ii_r - jj_r + 6.f * ij_r) * (1.f / 30.f);
                     t6[5] = (2.f * ii_i - jj_i + 6.f * ij_i) * (1.f / 30.f);
                 }
+                float ws[6];
                 #pragma unroll
-                for (int q = 0; q < 6; q++) {
-                    const float wsum = warp_sum(t6[q]);
-                    if (lane == 0) atomicAdd(g.tcf_out + (size_t)bz * g.tcf_sout + q, (double)wsum);
+                for (int q = 0; q < 6; q++) ws[q] = warp_sum(t6[q]);
+                if (lane == 0) {
+                    #pragma unroll
+                    for (int q = 0; q < 6; q++) atomicAdd(&tred[a][q], (double)ws[q]);
+                    __threadfence_block();
+                    if (atomicAdd(&tcnt[a], 1) == PEW - 1) {   // the tile's last epilogue warp
+                        __threadfence_block();
+                        #pragma unroll
+                        for (int q = 0; q < 6; q++) {   // every other warp's add precedes its count
+                            volatile double *slot = &tred[a][q];
+                            const double tot = *slot;
+                            *slot = 0.0;
+                            atomicAdd(g.tcf_out + (size_t)bz * g.tcf_sout + q, tot);
+                        }
+                        atomicExch(&tcnt[a], 0);
+                    }
                 }
             }
+            // the accumulator (and tred[a]) is free for tile i + 2 once every warp is done
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[a]);
         }
     }
     fence_before();
