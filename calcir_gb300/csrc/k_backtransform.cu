@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a, BtSplit sp) {
     const int t = threadIdx.x;
     if (t < BT_NB) tau[t] = t < nbb ? tau_g[kb + t] : 0.f;
 
-    // G = V_b^T V_b: thread (tx, ty) accumulates G[ty + 16 p][tx + 16 q]
+    // G = V_b^T V_b: thread (tx, ty) accumulates G[ty + 16 p][tx + 16 q] for p <= q only: the
+    // T recursion reads G above the diagonal, and the tiles p > q lie strictly below it
     {
         const int tx = t & 15, ty = t >> 4;
         float acc[8][8];
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a, BtSplit sp) {
                 for (int q = 0; q < 8; q++) {
                     const float4 vb = *reinterpret_cast<const float4 *>(Vt + (tx + 16 * q) * BT_LDV + rr);
                     #pragma unroll
-                    for (int p = 0; p < 8; p++)
+                    for (int p = 0; p <= q; p++)
                         acc[p][q] = fmaf(va[p].x, vb.x, fmaf(va[p].y, vb.y, fmaf(va[p].z, vb.z, fmaf(va[p].w, vb.w, acc[p][q]))));
                 }
             }
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a, BtSplit sp) {
         #pragma unroll
         for (int p = 0; p < 8; p++)
             #pragma unroll
-            for (int q = 0; q < 8; q++) M[(ty + 16 * p) * BT_LDM + tx + 16 * q] = acc[p][q];
+            for (int q = p; q < 8; q++) M[(ty + 16 * p) * BT_LDM + tx + 16 * q] = acc[p][q];
     }
     __syncthreads();
     // T, column by column; T[i][l] (i <= l) is kept at M[l][i], which the recursion never
