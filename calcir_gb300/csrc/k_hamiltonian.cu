@@ -145,9 +145,15 @@ __device__ __forceinline__ float pair_coupling(const Chrom &lo, const Chrom &hi,
 
 constexpr int HT = 32;   // tile edge
 __global__ void __launch_bounds__(HT * 8) k_hmatrix(BuildArgs a) {
+    // H is symmetric and each coupling is evaluated in canonical order (the lower index
+    // first), so a tile above the diagonal is computed once and written twice: directly and,
+    // through shared memory, transposed into its mirror tile; tiles below the diagonal return
+    if (blockIdx.y > blockIdx.x) return;
     __shared__ Chrom rows[HT], cols[HT];
+    __shared__ float tile[HT][HT + 1];
     const int f = blockIdx.z;
     const int r0 = blockIdx.y * HT, c0 = blockIdx.x * HT;
+    const bool mirror = blockIdx.y < blockIdx.x;
     const float *ct = a.ct + (size_t)f * CT_NROW * a.ld;
     const int tid = threadIdx.y * HT + threadIdx.x;
     if (tid < 2 * HT) {
@@ -177,6 +183,16 @@ __global__ void __launch_bounds__(HT * 8) k_hmatrix(BuildArgs a) {
         else if (r < c) h = pair_coupling(rows[rl], cols[threadIdx.x], bx, by, bz, a.maps, a.ispecies);
         else h = pair_coupling(cols[threadIdx.x], rows[rl], bx, by, bz, a.maps, a.ispecies);
         H[(size_t)r * a.ldh + c] = h;
+        tile[rl][threadIdx.x] = h;
+    }
+    if (!mirror) return;
+    __syncthreads();
+    // the mirror tile: H[c0 + j][r0 + l] = H[r0 + l][c0 + j], written along r0 + l
+    const int rm = r0 + threadIdx.x;
+    #pragma unroll
+    for (int i = 0; i < HT / 8; i++) {
+        const int jl = threadIdx.y + 8 * i, cm = c0 + jl;
+        if (cm < a.n && rm < a.n) H[(size_t)cm * a.ldh + rm] = tile[threadIdx.x][jl];
     }
 }
 
