@@ -378,6 +378,10 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     a.status = c->buf[B_STATUS].as<int>();
     a.sweeps = c->buf[B_SWEEPS].as<unsigned long long>();
     a.nchrom_mol = c->p.nchrom_mol;
+    // the mixed forms run the eigensolver's products on the tensor cores as split BF16, as
+    // the whole-job path does
+    a.precision = c->p.precision == CIR_PREC_FP32 ? CIR_PREC_FP32 : CIR_PREC_BF16X3;
+    a.err = c->buf[B_ERR].as<int>();
     if (eigh_profiling()) {
         CK(c->buf[B_PROF].ensure((size_t)nmat * CIR_EIG_PROF_SLOTS * 8));
         CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
@@ -400,6 +404,7 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     c->stats.eig_sweeps += (long long)sweeps;
     for (int i = 0; i < nmat; i++)
         if (st[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached on matrix %d", i);
+    if (a.precision != CIR_PREC_FP32 && (rc = check_kernel_flag(c))) return rc;
     return CIR_OK;
 }
 

@@ -590,9 +590,9 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
         e = KM <= 64 ? merge(k_dc_merge<64>, 64) : KM <= 128 ? merge(k_dc_merge<128>, 128)
           : KM <= 512 ? merge(k_dc_merge<DC_NT>, DC_NT) : merge(k_dc_merge<2 * DC_NT>, 2 * DC_NT);
         if (e != cudaSuccess) return e;
-        // the top two levels of the mixed forms on the tensor cores: one batched product per
+        // the top three levels of the mixed forms on the tensor cores: one batched product per
         // merge half when every offset keeps 16-byte alignment
-        bool tc = a.precision != CIR_PREC_FP32 && level <= 1;
+        bool tc = a.precision != CIR_PREC_FP32 && level <= 2;
         for (int b = 0; tc && b < (1 << level); b++)
             tc = (dc_off(level, b, n) & 3) == 0 && (dc_off(level + 1, 2 * b + 1, n) & 3) == 0;
         if (tc) {
