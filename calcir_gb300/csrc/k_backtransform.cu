@@ -233,15 +233,31 @@ __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a, BtSplit sp) {
 }
 
 // Q as a split pair in the same layout (column c at Q[c*ld ..], rows 0..n-1).
-__global__ void k_bt_split_q(const float *Q, long long sQ, int n, int ld, SplitMat Qs, long long sS) {
-    const int c = blockIdx.x, mat = blockIdx.y;
-    const float *q = Q + (size_t)mat * sQ + (size_t)c * ld;
-    const size_t o = (size_t)mat * sS + (size_t)c * ld;
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        const float x = q[r];
-        const __nv_bfloat16 h = __float2bfloat16_rn(x);
-        Qs.hi[o + r] = h;
-        Qs.lo[o + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+// Q as a split pair (the same layout, rows of ld), eight rows per block: 16-byte loads and
+// 8-byte stores of four BF16; values past n are zero.  ld is a multiple of 8 on this path.
+constexpr int BT_SQ_ROWS = 8;
+
+__global__ void __launch_bounds__(256) k_bt_split_q(const float *Q, long long sQ, int n, int ld, SplitMat Qs,
+                                                    long long sS) {
+    const int mat = blockIdx.y, n4 = (n + 3) >> 2, c0 = blockIdx.x * BT_SQ_ROWS;
+    for (int idx = threadIdx.x; idx < BT_SQ_ROWS * n4; idx += blockDim.x) {
+        const int cr = idx / n4, r = 4 * (idx - cr * n4), c = c0 + cr;
+        if (c >= n) break;
+        float4 x = *reinterpret_cast<const float4 *>(Q + (size_t)mat * sQ + (size_t)c * ld + r);
+        if (r + 1 >= n) x.y = 0.f;
+        if (r + 2 >= n) x.z = 0.f;
+        if (r + 3 >= n) x.w = 0.f;
+        const __nv_bfloat162 h0 = __floats2bfloat162_rn(x.x, x.y), h1 = __floats2bfloat162_rn(x.z, x.w);
+        const __nv_bfloat162 l0 = __floats2bfloat162_rn(x.x - __bfloat162float(h0.x), x.y - __bfloat162float(h0.y));
+        const __nv_bfloat162 l1 = __floats2bfloat162_rn(x.z - __bfloat162float(h1.x), x.w - __bfloat162float(h1.y));
+        const size_t o = (size_t)mat * sS + (size_t)c * ld + r;
+        uint2 hv, lv;
+        hv.x = *reinterpret_cast<const uint32_t *>(&h0);
+        hv.y = *reinterpret_cast<const uint32_t *>(&h1);
+        lv.x = *reinterpret_cast<const uint32_t *>(&l0);
+        lv.y = *reinterpret_cast<const uint32_t *>(&l1);
+        *reinterpret_cast<uint2 *>(Qs.hi + o) = hv;
+        *reinterpret_cast<uint2 *>(Qs.lo + o) = lv;
     }
 }
 
@@ -260,7 +276,7 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
         return SplitMat{b, b + ms};
     };
     const SplitMat Qs = pair(P), Vs = pair(Q), Ys = pair(a.Z), Ps = pair(U);
-    k_bt_split_q<<<dim3(n, nmat), 256, 0, s>>>(Q, ms, n, ld, Qs, ss);
+    k_bt_split_q<<<dim3((n + BT_SQ_ROWS - 1) / BT_SQ_ROWS, nmat), 256, 0, s>>>(Q, ms, n, ld, Qs, ss);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const size_t smem = bt_prep_smem();
