@@ -80,6 +80,21 @@ def test_eigh_random(lib, n):
         _check_eig(A[m], w[m], V[m])
 
 
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_eigh_rejects_non_finite_host_matrices(lib, bad):
+    """A NaN or infinity in a host matrix is an error before any GPU work (the host check of
+    cir_eigh); the context stays usable."""
+    from calcir_gb300 import CirError
+    rng = np.random.default_rng(3)
+    A = np.stack([_sym(rng, 40) for _ in range(2)])
+    A[1, 7, 3] = A[1, 3, 7] = bad
+    with lib.Engine(lib.default_params(species="H2O"), 8) as eng:
+        with pytest.raises(CirError, match="NaN or Inf"):
+            eng.eigh(A)
+        w, V = eng.eigh(A[:1])
+    _check_eig(A[0], w[0], V[0])
+
+
 @pytest.mark.parametrize("n", [96, 302])
 def test_eigh_special_matrices(lib, n):
     """Zero, scaled identity, exact ties, a rank-one perturbation, diagonal, and a
