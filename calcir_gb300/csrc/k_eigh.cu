@@ -58,6 +58,8 @@ __device__ __forceinline__ void cp_async16(float *dst, const float *src, bool va
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// request the 128-byte line holding p into L2 (no data returned, no register held)
+__device__ __forceinline__ void prefetch_l2(const float *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
@@ -577,10 +579,14 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
                 while (Jj > Ii) { Jj -= Ii + 1; Ii++; }
                 for (int q = warp; q < ntiles; q += NW) {
                     const int I = j0 + Ii, J = j0 + Jj;
+                    Jj += NW;                // this warp's next tile, whose lines are requested
+                    while (Jj > Ii) { Jj -= Ii + 1; Ii++; }   // into L2 before this one is read
+                    if (q + NW < ntiles) {
+                        const int c = 32 * (j0 + Jj) + lane;
+                        if (c < n) prefetch_l2(A + (size_t)c * ld + 32 * (j0 + Ii));
+                    }
                     if (I == J || 32 * I + 32 > n) symv_tile<true>(A, ld, n, I, J, x, ywp, lane);
                     else symv_tile<false>(A, ld, n, I, J, x, ywp, lane);
-                    Jj += NW;
-                    while (Jj > Ii) { Jj -= Ii + 1; Ii++; }
                 }
             }
             mark(14);
