@@ -243,8 +243,7 @@ __device__ int dc_root(int i, int Kp, const float *Dn, const float *z2, float rh
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, const float *Qin, float *Mscr,
-                                                    float *Uout) {
+__global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, const float *Qin, float *Uout) {
     extern __shared__ __align__(16) float sm[];
     const DcSmem L(KM);
     float *D = sm + L.D, *Ds = sm + L.Ds, *zs = sm + L.zs, *z2 = sm + L.z2, *Dn = sm + L.Dn, *tau = sm + L.tau;
@@ -276,7 +275,6 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
     float *dw = a.DE + (size_t)mat * 3 * ld;
     const float beta = dw[ld + mid - 1];
     const float *Q = Qin + (size_t)mat * a.mstride;
-    float *M = Mscr + (size_t)mat * a.mstride;      // row-major K x K at M + (a0+s)*ld + a0
     float *U = Uout + (size_t)mat * a.mstride;
     const float rho = 2.f * fabsf(beta);
     const float sgn = beta >= 0.f ? 1.f : -1.f;
@@ -411,47 +409,48 @@ __global__ void __launch_bounds__(NT) k_dc_merge(EighArgs a, int level, int KM, 
     }
     __syncthreads();
     mark(10);
-    // M = G W in the sorted basis (row-major), then U = P M; without deflation rotations
-    // (G = I) the columns go straight to U
-    if (nrot == 0) {
-        for (int c = tid; c < K; c += NT) {
-            const int q = src[c];
-            if (q < Kp) {
-                const float base = Dn[org[q]], ti = tau[q], sc = inv[q];
-                for (int r = 0; r < K; r++) {
-                    const int jn = kind[r];
-                    U[(size_t)(a0 + perm[r]) * ld + a0 + c] = jn >= 0 ? zh[jn] / ((Dn[jn] - base) - ti) * sc : 0.f;
-                }
-            } else {
-                const int p = defl[q - Kp];
-                for (int r = 0; r < K; r++) U[(size_t)(a0 + perm[r]) * ld + a0 + c] = r == p ? 1.f : 0.f;
-            }
-        }
-        mark(11);
-        return;
+    // U = P G W without an intermediate: G = G_0 G_1 ... G_{nrot-1} are the deflation
+    // rotations (G_t mixes the sorted rows p_t, j_t: p' = c p - s j, j' = s p + c j), W the
+    // secular vectors in the sorted basis; rows that no rotation touches take W directly.
+    // The deflation scan leaves the rotations in chains: rotation t+1 continues the chain of
+    // rotation t when p_{t+1} = j_t, and no other rotation touches p_t or j_t.  Applied from
+    // the last to the first, rotation t therefore reads row p_t from W and row j_t from the
+    // previous step's p row (or from W at the end of a chain); row j_t is then final, and
+    // row p_t is carried to rotation t-1 or, at the start of a chain, written.  The values
+    // and the order of the operations are those of applying every rotation to a full copy.
+    int *touched = reinterpret_cast<int *>(D);   // D is free once the two lists are merged
+    const int *rotp = reinterpret_cast<const int *>(rot);
+    for (int r = tid; r < K; r += NT) touched[r] = 0;
+    __syncthreads();
+    for (int t = tid; t < nrot; t += NT) {
+        touched[rotp[4 * t]] = 1;
+        touched[rotp[4 * t + 1]] = 1;
     }
+    __syncthreads();
     for (int c = tid; c < K; c += NT) {
         const int q = src[c];
-        if (q < Kp) {
-            const float base = Dn[org[q]], ti = tau[q], sc = inv[q];
-            for (int r = 0; r < K; r++) {
-                const int jn = kind[r];
-                M[(size_t)(a0 + r) * ld + a0 + c] = jn >= 0 ? zh[jn] / ((Dn[jn] - base) - ti) * sc : 0.f;
-            }
-        } else {
-            const int p = defl[q - Kp];
-            for (int r = 0; r < K; r++) M[(size_t)(a0 + r) * ld + a0 + c] = r == p ? 1.f : 0.f;
-        }
+        const bool root = q < Kp;
+        const float base = root ? Dn[org[q]] : 0.f, ti = root ? tau[q] : 0.f, sc = root ? inv[q] : 0.f;
+        const int pd = root ? -1 : defl[q - Kp];
+        auto w = [&](int r) -> float {   // W[r][c]: secular vector entry, or the deflated unit vector
+            if (!root) return r == pd ? 1.f : 0.f;
+            const int jn = kind[r];
+            return jn >= 0 ? zh[jn] / ((Dn[jn] - base) - ti) * sc : 0.f;
+        };
+        float *Uc = U + (size_t)a0 * ld + a0 + c;
+        for (int r = 0; r < K; r++)
+            if (!touched[r]) Uc[(size_t)perm[r] * ld] = w(r);
+        float carry = 0.f;
         for (int t = nrot - 1; t >= 0; t--) {
-            const int p = reinterpret_cast<const int *>(rot)[4 * t], j = reinterpret_cast<const int *>(rot)[4 * t + 1];
+            const int p = rotp[4 * t], j = rotp[4 * t + 1];
             const float cc = rot[4 * t + 2], ss = rot[4 * t + 3];
-            float *mp = M + (size_t)(a0 + p) * ld + a0 + c, *mj = M + (size_t)(a0 + j) * ld + a0 + c;
-            const float rp = *mp, rj = *mj;
-            *mp = cc * rp - ss * rj;
-            *mj = ss * rp + cc * rj;
+            const float rp = w(p), rj = (t + 1 < nrot && rotp[4 * (t + 1)] == j) ? carry : w(j);
+            carry = cc * rp - ss * rj;
+            Uc[(size_t)perm[j] * ld] = ss * rp + cc * rj;
+            if (t == 0 || rotp[4 * (t - 1) + 1] != p) Uc[(size_t)perm[p] * ld] = carry;
         }
-        for (int r = 0; r < K; r++) U[(size_t)(a0 + perm[r]) * ld + a0 + c] = M[(size_t)(a0 + r) * ld + a0 + c];
     }
+    mark(11);
     (void)nd;
 }
 
@@ -584,7 +583,7 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
         auto merge = [&](auto kern, int nt) -> cudaError_t {
             cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (r != cudaSuccess) return r;
-            kern<<<dim3(1 << level, nmat), nt, smem, s>>>(a, level, KM, buf[cur], buf[other], buf[2]);
+            kern<<<dim3(1 << level, nmat), nt, smem, s>>>(a, level, KM, buf[cur], buf[2]);
             return cudaSuccess;
         };
         e = KM <= 64 ? merge(k_dc_merge<64>, 64) : KM <= 128 ? merge(k_dc_merge<128>, 128)
