@@ -115,6 +115,26 @@ def test_eigh_special_matrices(lib, n):
         _check_eig(A, w[m], V[m])
 
 
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("n", [300, 1024])
+def test_eigh_clustered_spectrum(lib, n, precision):
+    """Eigenvalues in tight clusters (members 1e-4 apart, 1e-7 of the norm, up to 24 per
+    cluster): every merge deflates long runs of consecutive close pairs by Givens rotations,
+    which it applies to U as chains with one carried value per column.  The eigenpairs meet
+    the bounds of the random matrices."""
+    rng = np.random.default_rng(n + 11)
+    lam = []
+    while len(lam) < n:
+        c = rng.uniform(-1000.0, 1000.0)
+        lam.extend(c + 1e-4 * np.arange(min(int(rng.integers(1, 25)), n - len(lam))))
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A = (Q * np.asarray(lam)) @ Q.T
+    A = ((A + A.T) / 2).astype(np.float32)
+    with lib.Engine(lib.default_params(species="H2O", precision=precision), 8) as eng:
+        w, V = eng.eigh(A[None])
+    _check_eig(A, w[0], V[0])
+
+
 def test_propagate(lib):
     rng = np.random.default_rng(1)
     n, nprop, dt = 200, 3, 0.010
