@@ -1,4 +1,4 @@
-"""Arithmetic peaks that the generated peak file does not hold: FP32 on the SIMT pipe
+"""Arithmetic peaks that MEASURED_PEAKS.json (HBM copy and BF16 GEMM) does not hold: FP32 on the SIMT pipe
 (cuBLAS SGEMM with TF32 off), TF32 on the tensor cores and FP64, each as the best of a few
 back-to-back cuBLAS GEMMs timed with CUDA events.  They are the denominators of the plain
 form's FP32 rooflines (SIMT propagation GEMMs, merge and back-transform products) and of the
