@@ -12,9 +12,11 @@ correlation points at 10 fs = 2500 frame-steps, on seeded synthetic frames.
   e2e    the same through cir_run with pinned host buffers: positions copied in and all
          results copied out inside the timed region
 
---impl reference times the reference's per-frame algorithm (build, ssyevd, three complex
-GEMMs, 15 gemv/dot pairs) on the host cores, the only form of the reference that runs on
-the GPU machine (it needs MAGMA and libxdrfile, which are not installed there).
+--impl reference times the reference's per-frame algorithm (build, LAPACK dsyevd, three
+complex GEMMs, 15 gemv/dot pairs) on the host cores, on the timed job's own frames and
+origins, the only form of the reference that runs on the GPU machine (it needs MAGMA and
+libxdrfile, which are not installed there).  That arm loads no compiled code of this
+repository: its frames come from the numpy restatement of the generator.
 """
 from __future__ import annotations
 
@@ -127,16 +129,13 @@ def gpu_identifier():
     return None
 
 
-def profiled_traffic():
-    """DRAM bytes per 1024 x 1024 matrix of the tridiagonalisation kernel, from the committed
-    ncu summary (profiles/k_eigh_tq_n1024.md, line 'dram_bytes_per_matrix: <B>')."""
-    try:
-        for line in open(os.path.join(ROOT, "profiles", "k_eigh_tq_n1024.md")):
-            if line.startswith("dram_bytes_per_matrix:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except (OSError, ValueError, IndexError):
-        pass
-    return None
+# DRAM bytes (read + write) per 1024 x 1024 matrix of the tridiagonalisation kernel, from one
+# ncu capture of k_eigh_tq on 152 matrices of order 1024 (dram__bytes_read.sum +
+# dram__bytes_write.sum over the launch, / 152):
+#   python -m calcir_gb300.profile eigh --nmol 512 --batch 152 && \
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_eigh_tq -c 1 \
+#       python -m calcir_gb300.profile eigh --nmol 512 --batch 152
+TRIDIAG_DRAM_BYTES_PER_MATRIX = 0.666e9
 
 
 def tridiag_bytes(n, nb=32):
@@ -148,6 +147,27 @@ def tridiag_bytes(n, nb=32):
     return sym + upd + 8.0 * 2 * 2   # + the final 2 x 2 block
 
 
+PARITY_FIXTURE = os.path.join(ROOT, "tests", "golden", "fullsize_512h2o.npz")
+PARITY_KEYS = ("tcf_ir", "tcf_vv", "tcf_vh", "ls_ir", "ls_vv", "ls_vh", "sw")
+
+
+def parity(out, seed, bound):
+    """Relative L2 error of each spectrum of a timed job against the FP64 oracle's spectra of
+    the same job (512 H2O, 10 origins x 250 points, frames of seed 1), stored as a fixture
+    by tests/golden/make_fullsize.py."""
+    if seed != 1 or not os.path.exists(PARITY_FIXTURE):
+        return {"note": "no oracle fixture for this seed"}
+    z = np.load(PARITY_FIXTURE)
+    errs = {}
+    for k in PARITY_KEYS:
+        a, b = np.asarray(out[k]), z["fin_" + k]
+        if a.shape != b.shape:
+            return {"note": f"{k}: shape {a.shape} != fixture {b.shape}"}
+        errs[k] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return {"vs": "FP64 oracle, the same job (tests/golden/fullsize_512h2o.npz)", "rel_l2": errs,
+            "bound": bound, "within_bound": all(v < bound for v in errs.values())}
+
+
 def make_frames(cg, seed):
     p = cg.default_params(**JOB)
     fos = cg.frame_table(p, 0.010)
@@ -155,35 +175,61 @@ def make_frames(cg, seed):
     return p, xyz, box, fos
 
 
-def cpu_port_rate(seed, steps_per_sample, repeats):
-    """Frame-steps/s of the reference algorithm on the host cores (oracle/cpu_reference)."""
-    import calcir_gb300 as cg
-    from oracle import cpu_reference as R
-    xyz, box = cg.synth_trajectory(NMOL, steps_per_sample, seed=seed)
-    prm = {"natom_mol": 4, "nchrom_mol": 2, "imodel": 1, "ispecies": 0, "map": 0, "avef": JOB["avef"],
-           "dt": JOB["dt"]}
-    R.time_frame_steps(xyz, box, prm, 2)   # warm-up (threads, page faults)
-    rates = []
-    for _ in range(repeats):
-        sec, cores = R.time_frame_steps(xyz, box, prm, steps_per_sample)
-        rates.append(steps_per_sample / sec)
-    return rates, R.host_cores()
+# the configuration both arms report (the reference arm times the same job's frame-steps)
+CONFIG = {"workload": WORKLOAD, "nmol": NMOL, "nchrom": 2 * NMOL, "nsamples": JOB["nsamples"],
+          "ntcfpoints": JOB["ntcfpoints"], "seed": 1,
+          "l2": "no flush needed: each step streams ~20 GB of Hamiltonians and eigenvectors (>> 129 MB L2)"}
+CPU_FORM = ("reference algorithm on the host cores (oracle/cpu_reference.py): build, LAPACK dsyevd in FP64 "
+            "(scipy, evd driver), dense propagator + 3 complex64 cgemm, 15 cgemv/cdotu; frames from the numpy "
+            "restatement of the seeded generator (oracle/synth.py)")
+
+
+class CpuPort:
+    """The reference algorithm on the host cores, on the frames of the timed job (seed 1 +
+    rank): frames come from oracle/synth.py, which loads no compiled code of this
+    repository.  One sample = the first `per` frame-steps of one time origin; successive
+    samples walk the job's 10 origins."""
+
+    def __init__(self, seed, per):
+        from oracle import oracle as O
+        from oracle import synth
+        self.per = per
+        self.prm = {"natom_mol": 4, "nchrom_mol": 2, "imodel": 1, "ispecies": 0, "map": JOB["map"],
+                    "avef": JOB["avef"], "dt": JOB["dt"], "sampleEvery": JOB["sampleEvery"], "beginTime": 0.0}
+        K = JOB["ntcfpoints"]
+        self.tables = [[O.frame_index(self.prm, 0.010, s, k) for k in range(per)] for s in range(JOB["nsamples"])]
+        nframes = max(t[-1] for t in self.tables) + 1
+        assert per <= K
+        self.xyz, self.box = synth.trajectory(NMOL, nframes, seed=seed)
+        self.i = 0
+
+    def sample(self):
+        """(frame-steps per second, host threads) of the next sample."""
+        from oracle import cpu_reference as R
+        table = self.tables[self.i % len(self.tables)]
+        self.i += 1
+        sec, cores = R.time_origin(self.xyz, self.box, self.prm, table, self.per)
+        return self.per / sec, cores
 
 
 def run_reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    per = args.cpu_sample
-    warm, _ = cpu_port_rate(args.seed, per, max(args.warmup, 0))
-    rates, cores = cpu_port_rate(args.seed, per, args.steps)
-    value = float(np.mean(rates))
-    sample = (f"{per} consecutive frame-steps of one origin of the workload (1024 chromophores) per step, "
-              "numpy FP32 ssyevd + complex64 GEMMs on the host cores")
+    port = CpuPort(args.seed, args.cpu_sample)
+    for _ in range(max(args.warmup, 0)):
+        port.sample()
+    rates, cores = [], 1
+    for _ in range(args.steps):
+        r, cores = port.sample()
+        rates.append(r)
+    value = float(len(rates) / np.sum(1.0 / np.asarray(rates)))     # total frame-steps / total seconds
+    sample = (f"{args.cpu_sample} consecutive frame-steps (k = 0..{args.cpu_sample - 1}) of one time origin per "
+              f"step, the steps walking the job's {JOB['nsamples']} origins; " + CPU_FORM)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per / value * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": "reference algorithm on the host CPU"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.cpu_sample / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 eig + c64 gemm",
+            "data": "synthetic", "config": CONFIG, "form": "reference algorithm on the host CPU",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -381,12 +427,13 @@ def main():
             t1 = torch.cuda.Event(enable_timing=True)
             t0.record(stream)
             for _ in range(steps):
-                eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+                out = eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
             t1.record(stream)
             torch.cuda.synchronize()
             barrier()
             res["clk"] = sampler.stop() if sampler else None
             res["ms"] = t0.elapsed_time(t1)
+            res["out"] = out
             res["stats"] = eng.stats()
             if e2e:
                 torch.cuda.synchronize()
@@ -449,9 +496,7 @@ def main():
         "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else f"f32+{args.precision}",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": form, "nsamples": 10, "ntcfpoints": 250,
-                   "nchrom": n, "l2": "no flush needed: each step streams ~20 GB of Hamiltonians and eigenvectors "
-                                     "(>> 129 MB L2)"},
+        "config": CONFIG, "form": form,
         "stages_ms_per_step": {k: st[k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(st["kernel_launches"]),
@@ -462,8 +507,8 @@ def main():
                              "32-column panel one read and write of the trailing lower triangle; "
                              f"{tridiag_bytes(n) / 1e9:.3f} GB per 1024 x 1024 matrix x 2500 matrices per launch",
                      "ms_per_launch": tq_ms,
-                     "traffic": (profiled_traffic() * steps_per_job) if profiled_traffic() else None,
-                     "traffic_note": "ncu dram__bytes_read+write per matrix (profiles/k_eigh_tq_n1024.md) x 2500"},
+                     "traffic": TRIDIAG_DRAM_BYTES_PER_MATRIX * steps_per_job,
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per matrix x 2500"},
         "roofline_eigensolver": {"kernels": "tridiagonalisation, divide and conquer, blocked Householder "
                                             "back-transform V = Q_H Q_T",
                                  "achieved": eig_tflops, "unit": "TFLOP/s",
@@ -483,8 +528,9 @@ def main():
         line["options"] = dict(options, note="same results by less work (frame sharing across the overlapping "
                                              "origins; propagating psi = F m(0) instead of F), reported beside the "
                                              "headline, which does the reference's full work")
+    line["parity"] = parity(main_res["out"], args.seed + rank, 1e-4 if args.precision == "fp32" else 1e-3)
     if plain is not None:
-        line["plain_fp32"] = {"value": total_steps / (plain["ms"] * 1e-3) / world * world, "unit": UNIT,
+        line["plain_fp32"] = {"parity": parity(plain["out"], args.seed + rank, 1e-4),"value": total_steps / (plain["ms"] * 1e-3) / world * world, "unit": UNIT,
                               "ms_per_step": plain["ms"] / args.steps,
                               "stages_ms_per_step": {k: plain["stats"][k] / args.steps for k in ("ms_build", "ms_eig", "ms_prop")},
                               "mixed_over_plain": plain["ms"] / ms}
@@ -504,10 +550,14 @@ def main():
                 "peak": extra["fp32_simt_tflops"], "unit": "TFLOP/s", "frac": plain_prop / extra["fp32_simt_tflops"],
                 "peak_kind": "measured cuBLAS SGEMM, TF32 off (peaks_probe)"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rates, cores = cpu_port_rate(args.seed, args.cpu_sample, 2)
-        line["cpu_baseline"] = {"value": float(np.mean(rates)), "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"2 x {args.cpu_sample} frame-steps of one origin (1024 chromophores), "
-                                          "reference algorithm in numpy FP32 on the host cores"}
+        port = CpuPort(args.seed, args.cpu_sample)
+        port.sample()                                   # warm-up (threads, page faults)
+        got = [port.sample() for _ in range(2)]
+        rates = np.asarray([r for r, _ in got])
+        line["cpu_baseline"] = {"value": float(2 / np.sum(1.0 / rates)), "unit": UNIT,
+                                "cores": got[-1][1], "kind": "port",
+                                "sample": f"2 x {args.cpu_sample} frame-steps (origins 1 and 2 of the job); "
+                                          + CPU_FORM}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -44,6 +44,7 @@ class Params(C.Structure):
         ("precision", C.c_int), ("batch_frames", C.c_int), ("verbose", C.c_int),
         ("cuda_graphs", C.c_int), ("autotune", C.c_int),
         ("propagate_vectors", C.c_int), ("share_frames", C.c_int), ("refine_eigen", C.c_int),
+        ("test_stall_gemm", C.c_int), ("test_sweep_cap", C.c_int),
     ]
 
 

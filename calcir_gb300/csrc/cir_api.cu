@@ -382,6 +382,8 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     // the whole-job path does
     a.precision = c->p.precision == CIR_PREC_FP32 ? CIR_PREC_FP32 : CIR_PREC_BF16X3;
     a.err = c->buf[B_ERR].as<int>();
+    a.test_stall = c->p.test_stall_gemm;
+    a.test_sweep_cap = c->p.test_sweep_cap;
     if (eigh_profiling()) {
         CK(c->buf[B_PROF].ensure((size_t)nmat * CIR_EIG_PROF_SLOTS * 8));
         CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
@@ -848,6 +850,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         // eigensolver's tensor-core products as 3-pass split BF16
         e.precision = p.precision == CIR_PREC_FP32 ? CIR_PREC_FP32 : CIR_PREC_BF16X3;
         e.err = c->buf[B_ERR].as<int>();
+        e.test_stall = c->p.test_stall_gemm;
+        e.test_sweep_cap = c->p.test_sweep_cap;
         e.tq_done = ev[5];
         e.avef = p.avef;
         e.omegaStart = p.omegaStart;
@@ -910,6 +914,7 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                     s1.epilogue = 1; s1.w = W + mk * ld; s1.wstride = dlt * ld;
                     s1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
                     s1.err = c->buf[B_ERR].as<int>();
+                    s1.test_stall = p.test_stall_gemm;
                     SplitGemmArgs s2 = s1;
                     s2.Ahi = Vr.hi; s2.Alo = Vr.lo;                                    // V
                     s2.Bhi = Gt.hi; s2.Blo = Gt.lo;
@@ -1318,6 +1323,8 @@ extern "C" int cir_loss_grad(cir_ctx *c, int nframes, const float *xyz, const fl
     e.nchrom_mol = p.nchrom_mol;
     e.precision = CIR_PREC_FP32;
     e.err = c->buf[B_ERR].as<int>();
+    e.test_stall = c->p.test_stall_gemm;
+    e.test_sweep_cap = c->p.test_sweep_cap;
     CK(cir_launch_eigh(e, nb, c->stream, &launches));
     // forward: psi(0) = m(0); psi(k) = U_k psi(k-1); correlation terms per step; checkpoints
     const long long sV = (long long)K * mstride, sWk = (long long)K * ld, sM = (long long)K * 9 * ld;

@@ -105,6 +105,9 @@ struct EighArgs {
     const float *Href;
     void *RW;
     int refine_iters, refine_chunk;
+    // fault drills (tests only, 0 = off): the split-BF16 GEMMs' stall (SplitGemmArgs::test_stall)
+    // and a cap on the QR sweeps of each divide-and-conquer leaf
+    int test_stall, test_sweep_cap;
 };
 
 // kernel launchers (return cudaError_t of the launch)
@@ -190,6 +193,8 @@ struct SplitGemmArgs {
     double *tcf_out;
     long long tcf_sout;
     int bz0;              // batch entry of blockIdx.z == 0 (set by the launcher when it splits a batch)
+    int test_stall;       // fault drill (tests only): 1 withholds the first tile's completion and
+                          // shortens the pipeline waits, so that they run out and raise err
 };
 size_t cir_split_ld(int n);   // leading dimension of the split operands (n rounded up to 8)
 cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches);

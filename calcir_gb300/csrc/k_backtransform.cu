@@ -295,6 +295,7 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
         g1.Chi = Ps.hi; g1.Clo = Ps.lo; g1.ldc = bw; g1.sC = ss; g1.out_mode = 1;
         g1.M = n; g1.N = nbb; g1.K = m;
         g1.err = a.err;
+        g1.test_stall = a.test_stall;
         SplitGemmArgs g2{};                                        // Z^T[:, kb:] -= P Y_b
         g2.Ahi = Ps.hi; g2.Alo = Ps.lo; g2.lda = bw; g2.sA = ss;
         g2.Bhi = Ys.hi + bt_yoff(b, n, bw); g2.Blo = Ys.lo + bt_yoff(b, n, bw); g2.ldb = bw; g2.sB = ss;
@@ -307,6 +308,7 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
         }
         g2.M = n; g2.N = m; g2.K = nbb;
         g2.err = a.err;
+        g2.test_stall = a.test_stall;
         if ((e = cir_launch_split_gemm(g1, nmat, s, &nl)) != cudaSuccess) return e;
         if ((e = cir_launch_split_gemm(g2, nmat, s, &nl)) != cudaSuccess) return e;
     }

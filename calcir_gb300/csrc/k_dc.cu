@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(128) k_dc_leaf(EighArgs a, int depth, float *Q
     for (int i = 0; i < s; i++) tn = fmaxf(tn, fabsf(d[i]) + 2.f * fabsf(e[i]));
     const float tiny = 1e-12f * tn + FLT_MIN;
     int cm = s - 1, nsweep = 0;
-    const int cap = 30 * s + 30;
+    const int cap = a.test_sweep_cap > 0 ? a.test_sweep_cap : 30 * s + 30;
     while (cm > 0 && nsweep < cap) {
         if (fabsf(e[cm - 1]) <= DC_EPS * (fabsf(d[cm - 1]) + fabsf(d[cm])) || fabsf(e[cm - 1]) <= tiny) {
             cm--;

@@ -1339,6 +1339,26 @@ void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];   // device address of g_noalloc_scrat
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// scratch bytes of a call on nmat matrices of order n (pad: A is copied to a 16-byte
+// aligned, ld-strided buffer first)
+size_t noalloc_need(int nmat, int n, bool pad) {
+    const int ld = (n + 3) & ~3;
+    const size_t mat = (size_t)n * ld * sizeof(float);
+    return align256(nmat * mat)                                   // Z
+           + align256(nmat * cir_eigh_rot_bytes(n))               // rotation groups
+           + align256(nmat * cir_eigh_de_bytes(ld))               // d, e, tau
+           + align256((size_t)nmat * sizeof(int))                 // status
+           + (pad ? align256(nmat * mat) : 0);                    // 16-byte aligned copy of A
+}
+
+// the largest order one call can take: a single matrix, with the aligned copy (pad) or
+// without it (then n is a multiple of 4)
+int noalloc_max_order(bool pad) {
+    int n = cir_eigh_max_n();
+    while (n > 1 && ((!pad && (n & 3)) || noalloc_need(1, n, pad) > NOALLOC_SCRATCH_BYTES)) n--;
+    return n;
+}
+
 }  // namespace
 
 extern "C" int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_stream) {
@@ -1372,11 +1392,14 @@ extern "C" int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_
     const int ld = (n + 3) & ~3;
     const bool pad = (ld != n) || (reinterpret_cast<uintptr_t>(A) & 15);
     const size_t mat = (size_t)n * ld * sizeof(float);
-    const size_t need = align256(nmat * mat)                                   // Z
-                        + align256(nmat * cir_eigh_rot_bytes(n))               // rotation groups
-                        + align256(nmat * cir_eigh_de_bytes(ld))               // d, e, tau
-                        + align256((size_t)nmat * sizeof(int))                 // status
-                        + (pad ? align256(nmat * mat) : 0);                    // 16-byte aligned copy of A
+    const size_t need = noalloc_need(nmat, n, pad);
+    if (noalloc_need(1, n, pad) > NOALLOC_SCRATCH_BYTES)
+        return cir_fail(CIR_ERR_ARG,
+                        "cir_eigh_noalloc: order %d needs %zu bytes of scratch for one matrix; the allocation-free "
+                        "scratch holds %zu bytes, enough for orders up to %d (%d when n is not a multiple of 4 or "
+                        "A is not 16-byte aligned)",
+                        n, noalloc_need(1, n, pad), NOALLOC_SCRATCH_BYTES, noalloc_max_order(false),
+                        noalloc_max_order(true));
     if (need > NOALLOC_SCRATCH_BYTES)
         return cir_fail(CIR_ERR_ARG,
                         "cir_eigh_noalloc: %d matrices of order %d need %zu bytes of scratch; the allocation-free "

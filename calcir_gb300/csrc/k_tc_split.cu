@@ -386,6 +386,9 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
     fence_after();
     const uint32_t tmem = *tslot;
     const int KT = (g.K + QK - 1) / QK;
+    // the pipeline's waits; the fault drill shortens them so that they run out quickly (the
+    // waits for copies and MMAs in flight before the CTA exits always keep the full limit)
+    const long long lim = g.test_stall ? (1ll << 14) : WAIT_LIMIT;
     auto fail = [&]() {
         *abort_flag = 1;
         if (g.err) atomicExch(g.err, 1);
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                 const int m0 = (rem / tiles_n) * QM, n0 = (rem % tiles_n) * QN;
                 for (int kt = 0; kt < KT; kt++, it++) {
                     const int s = it % QS;
-                    if (it >= QS && !(ok = mbar_wait(&empty[s], ((it / QS) & 1) ^ 1))) break;
+                    if (it >= QS && !(ok = mbar_wait(&empty[s], ((it / QS) & 1) ^ 1, lim))) break;
                     if (*abort_flag) break;
                     const uint32_t st = sbase + s * Q_STAGE;
                     mbar_expect_tx(&full[s], Q_STAGE);
@@ -421,13 +424,13 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             int li = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, li++) {
                 const int a = li & 1;
-                if (li >= 2 && !(ok = mbar_wait(&tempty[a], ((li >> 1) & 1) ^ 1))) break;
+                if (li >= 2 && !(ok = mbar_wait(&tempty[a], ((li >> 1) & 1) ^ 1, lim))) break;
                 if (*abort_flag) break;
                 fence_after();
                 const uint32_t d = tmem + (uint32_t)(a * QN);
                 for (int kt = 0; kt < KT; kt++, it++) {
                     const int s = it % QS;
-                    if (!(ok = mbar_wait(&full[s], (it / QS) & 1))) break;
+                    if (!(ok = mbar_wait(&full[s], (it / QS) & 1, lim))) break;
                     fence_after();
                     const uint32_t st = sbase + s * Q_STAGE;
                     #pragma unroll
@@ -443,7 +446,9 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                     mma_commit(&empty[s]);
                 }
                 if (!ok) break;
-                mma_commit(&tfull[a]);
+                // fault drill: the first tile's completion is never signalled, so the epilogue's
+                // wait on it (and then every other role's) runs out
+                if (!(g.test_stall && li == 0)) mma_commit(&tfull[a]);
             }
             if (!ok) fail();
             if (issued) {   // every MMA issued has completed before the accumulators are freed
@@ -458,7 +463,7 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
         int li = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
             const int a = li & 1;
-            if (!mbar_wait(&tfull[a], (li >> 1) & 1)) {
+            if (!mbar_wait(&tfull[a], (li >> 1) & 1, lim)) {
                 fail();
                 break;
             }

@@ -98,6 +98,14 @@ typedef struct cir_params {
        (Rayleigh quotients, first-order eigenvector correction and re-orthogonalisation;
        2 takes FP32 / split-BF16 eigenpairs to the accuracy of FP32 storage) */
     int   refine_eigen;
+    /* fault drills for tests, 0 (off) by default: each makes a bounded wait or iteration
+       cap of the GPU path run out on purpose, so that its error status can be checked
+       without faulting or hanging the GPU */
+    int   test_stall_gemm;         /* 1: the persistent split-BF16 GEMM withholds its first tile's
+                                      completion; its bounded waits (shortened to 2^14 polls) run
+                                      out and the call returns CIR_ERR_CUDA ("timed out") */
+    int   test_sweep_cap;          /* > 0: QR sweeps allowed per divide-and-conquer leaf; a cap the
+                                      leaves cannot meet makes cir_eigh return CIR_ERR_NOCONVERGE */
 } cir_params;
 
 /* Whole-job results, caller-owned host arrays sized by cir_result_sizes. */
@@ -198,14 +206,18 @@ int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w);
  * device and can fail mid-run.  This entry point allocates nothing: A [nmat][n][n] and
  * w [nmat][n] are the caller's DEVICE buffers (same meaning as cir_eigh), and all scratch
  * lives in one 8 MiB device array that every GPU which loads the library holds until the
- * process exits.  Requests whose scratch exceeds 8 MiB (more than one matrix of order
- * 1024, seven of order 512 or 25 of order 256 per call) are rejected with CIR_ERR_ARG;
- * split the batch instead.
- * The first call on a device looks up the array's device address (cudaGetSymbolAddress);
+ * process exits.  Requests whose scratch exceeds 8 MiB are rejected with CIR_ERR_ARG:
+ * orders above 1412 (above 1006 when n is not a multiple of 4 or A is not 16-byte
+ * aligned, since A is then copied into the scratch first), and batches of more than one
+ * matrix of order 1024, seven of order 512 or 25 of order 256 per call; split the batch
+ * instead.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress,
+ * which also loads the library's device code on that device under lazy module loading);
  * make that first call before any stream capture.  All calls share the one array and
  * every call overwrites it, so calls that overlap on the GPU (different streams or host
- * threads without ordering) race.  The call is issued on cuda_stream (NULL: the default
- * stream) and returns after that stream has finished it. */
+ * threads without ordering) race.  The call is synchronous: it is issued on cuda_stream
+ * (NULL: the default stream), reads the per-matrix convergence flags back with
+ * cudaMemcpyAsync into a host stack buffer and returns after cudaStreamSynchronize. */
 int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_stream);
 
 /* One propagation step of nprop independent chains: F <- V diag(exp(+i w dt/hbar)) V^T F,

@@ -19,8 +19,10 @@
 #     output prefix of at most 12 characters the write stays inside glibc's 24-byte
 #     minimum allocation, so the golden runs use short prefixes.
 # Usage: oracle/build_ref.sh [reference_dir]
+# The reference directory is the argument, else $CALCIR_REFERENCE_DIR, else the place the
+# reference sources are mounted read-only in the build container.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${CALCIR_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/calcIR.cu" ]; then

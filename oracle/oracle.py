@@ -192,14 +192,18 @@ def lineshape_rows(prm, y):
     return np.array(om), np.array(val)
 
 
-def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=False, mp=None):
-    """The whole job (main, calcIR.cu:360-839) in FP64.
+def accumulate(prm: dict, frames, boxes, frame_of_step, samples=None, propagate="psi", keep_frames=False,
+               mp=None):
+    """The per-frame loop of the job (main, calcIR.cu:360-760) in FP64, over the time origins
+    ``samples`` (default: all ``nsamples``): raw sums before the damping and normalisation.
 
     frames[f] is the (natoms, 3) position array of frame f, boxes[f] its box diagonal;
     frame_of_step[s*ntcf + k] selects the frame of step k of sample s.  propagate="full"
     carries the N x N matrix F like the reference; "psi" carries psi_a = F m_a(0) for the
-    nine vectors, the same numbers at O(N^2) per step."""
+    nine vectors, the same numbers at O(N^2) per step.  Sums of several calls over disjoint
+    origin sets add up to the sums of one call over their union (``merge``)."""
     S, K = prm["nsamples"], prm["ntcfpoints"]
+    samples = range(S) if samples is None else samples
     dt, t1, avef = float(F32(prm["dt"])), float(F32(prm["t1"])), float(F32(prm["avef"]))
     nom = nomega(prm)
     start, step = float(F32(prm["omegaStart"])), prm["omegaStep"]
@@ -214,7 +218,7 @@ def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=Fa
     ncm = prm["nchrom_mol"]
     per_frame = []
     N = None
-    for s in range(S):
+    for s in samples:
         for k in range(K):
             f = frame_of_step[s * K + k]
             E, H, dip, pol = frame(frames[f], boxes[f], prm, mp)
@@ -258,26 +262,55 @@ def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=Fa
             tcf[2, k] += vh
             if keep_frames:
                 per_frame.append({"E": E, "H": H, "lam": lam, "dip": dip, "pol": pol})
-    # damping and normalisation (calcIR.cu:777-839)
+    acc = {"tcf": tcf, "sw": Sw, "count": cnt, "ipr": ipr_acc, "mipr": mipr_acc, "oor": oor, "nchrom": N,
+           "omega": omega}
+    if keep_frames:
+        acc["frames"] = per_frame
+    return acc
+
+
+def merge(parts):
+    """Sum of the raw sums of ``accumulate`` calls over disjoint origin sets."""
+    out = dict(parts[0])
+    for p in parts[1:]:
+        for k in ("tcf", "sw", "count", "ipr", "mipr", "oor"):
+            out[k] = out[k] + p[k]
+    return out
+
+
+def finish(prm: dict, acc):
+    """Damping, normalisation, the C2R transforms and the lineshape rows (calcIR.cu:777-839,
+    890-919) of the raw sums over all ``nsamples`` origins."""
+    S, K = prm["nsamples"], prm["ntcfpoints"]
+    dt, t1 = float(F32(prm["dt"])), float(F32(prm["t1"]))
+    step = prm["omegaStep"]
+    N = acc["nchrom"]
     kk = np.arange(K)
     dcy = np.exp(-1.0 * kk * dt / (2.0 * t1)) / (1.0 * S)
-    tcf = tcf * dcy[None, :]
+    tcf = acc["tcf"] * dcy[None, :]
     n = K + prm["nzeros"]
     ls = [lineshape_rows(prm, c2r(tcf[q], n)) for q in range(3)]
     norm = N * S * K
+    cnt = acc["count"]
     with np.errstate(invalid="ignore", divide="ignore"):
         pw = cnt / step / norm
-        rw = (ipr_acc / step / norm) / pw
-        rmw = (mipr_acc / step / norm) / pw
+        rw = (acc["ipr"] / step / norm) / pw
+        rmw = (acc["mipr"] / step / norm) / pw
     out = {
         "tcf_ir": tcf[0], "tcf_vv": tcf[1], "tcf_vh": tcf[2],
-        "omega": omega, "sw": Sw / S, "pw": pw, "rw": rw, "rmw": rmw,
+        "omega": acc["omega"], "sw": acc["sw"] / S, "pw": pw, "rw": rw, "rmw": rmw,
         "ls_omega": ls[0][0], "ls_ir": ls[0][1], "ls_vv": ls[1][1], "ls_vh": ls[2][1],
-        "bins_out_of_range": oor, "count": cnt,
+        "bins_out_of_range": acc["oor"], "count": cnt,
     }
-    if keep_frames:
-        out["frames"] = per_frame
+    if "frames" in acc:
+        out["frames"] = acc["frames"]
     return out
+
+
+def run(prm: dict, frames, boxes, frame_of_step, propagate="psi", keep_frames=False, mp=None):
+    """The whole job (main, calcIR.cu:360-839) in FP64: ``accumulate`` over every time origin,
+    then ``finish``."""
+    return finish(prm, accumulate(prm, frames, boxes, frame_of_step, None, propagate, keep_frames, mp))
 
 
 def frame_index(prm, frame_dt, s, k):

@@ -10,6 +10,8 @@ parameter lines it prints (calcIR.cu:70-87).
 
 Run from the repository root (needs the reference sources and libcalcir.so):
     python tests/golden/make_golden.py [reference_dir]
+The reference directory is the argument, else $CALCIR_REFERENCE_DIR, else the default of
+oracle/build_ref.sh.  Each run works in a fresh temporary directory.
 """
 from __future__ import annotations
 
@@ -18,6 +20,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -26,7 +29,7 @@ sys.path.insert(0, ROOT)
 import calcir_gb300 as cg  # noqa: E402
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-WORK = os.path.join(ROOT, "_work", "golden_run")
+WORK = None   # set by main(): a fresh temporary directory per run
 
 # (case name, synthetic nmol, seed, input keys); frame_dt of every trajectory is 0.010 ps
 CASES = [
@@ -112,10 +115,11 @@ def run_parser_case(exe: str, name: str, text: str) -> None:
 
 
 def main() -> None:
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    exe = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), ref_dir], check=True,
-                         stdout=subprocess.PIPE, text=True).stdout.strip().splitlines()[-1]
-    os.makedirs(WORK, exist_ok=True)
+    global WORK
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CALCIR_REFERENCE_DIR")
+    cmd = [os.path.join(ROOT, "oracle", "build_ref.sh")] + ([ref_dir] if ref_dir else [])
+    exe = subprocess.run(cmd, check=True, stdout=subprocess.PIPE, text=True).stdout.strip().splitlines()[-1]
+    WORK = tempfile.mkdtemp(prefix="calcir_golden_")
     for name, nmol, seed, keys in CASES:
         run_case(exe, name, nmol, seed, keys)
     for name, text in PARSER_CASES.items():

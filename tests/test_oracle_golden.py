@@ -3,10 +3,12 @@
 The fixtures in tests/golden were written by the reference's own calcIR.cu built for the
 host (oracle/build_ref.sh, tests/golden/make_golden.py) on seeded synthetic trajectories.
 The reference runs in FP32; the oracle in FP64; spectra agree within 1e-4 relative L2."""
+import os
+
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, golden_params, load_golden
+from conftest import GOLDEN, GOLDEN_CASES, golden_params, load_golden
 from oracle import oracle as O
 
 TOL = 1e-4   # relative L2 per spectrum, FP32 reference vs FP64 oracle
@@ -69,3 +71,22 @@ def test_frequency_distributions(case):
         # NaN exactly where the histogram is empty (calcIR.cu:836-839)
         both = (out["count"] > 0) == (pw_ref > 0)
         assert np.mean(both) > 0.995
+
+
+@pytest.mark.parametrize("name", ["fullsize_512h2o", "fullsize_1024h2o"])
+def test_fullsize_fixture_finished_spectra(name):
+    """The finished spectra stored beside the raw sums of a full-length fixture (bench.py
+    reads them to state the error of its timed run) are what the oracle makes of the sums."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_fullsize as MF
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    prm, acc, _, _, fos = MF.load(path)
+    assert len(fos) == prm["nsamples"] * prm["ntcfpoints"]
+    fin = O.finish(prm, acc)
+    z = np.load(path)
+    for k in ("tcf_ir", "tcf_vv", "tcf_vh", "sw", "ls_ir", "ls_vv", "ls_vh"):
+        assert O.rel_l2(z["fin_" + k], fin[k]) < 1e-7, k
+    assert int(z["fin_ls_len"]) == len(fin["ls_omega"])
