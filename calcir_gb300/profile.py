@@ -5,6 +5,7 @@ CIR_EIGH_PROFILE=1 for the eigensolver's per-phase timers).
     python -m calcir_gb300.profile prop --n 1024 --nprop 10
     python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 250
     python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 50 --propagate-vectors 1
+    python -m calcir_gb300.profile grad --nmol 256 --nsamples 2 --ntcf 32
 
 Every stage goes through the C ABI (libcalcir.so)."""
 from __future__ import annotations
@@ -51,6 +52,18 @@ def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32", **options)
         print(f"run nmol {nmol}: {out['frame_steps_per_s']:.1f} frame-steps/s", eng.stats(), flush=True)
 
 
+def grad(nmol: int, nsamples: int, ntcf: int) -> None:
+    """One loss + gradient evaluation (cir_loss_grad): the adjoint kernels."""
+    p = cg.default_params(model="tip4p2005", species="H2O", ntcfpoints=ntcf, nsamples=nsamples, sampleEvery=2.0,
+                          avef=3415.0, omegaStart=2000, omegaStop=5000, omegaStep=1)
+    fos = cg.frame_table(p, 0.010)
+    xyz, box = cg.synth_trajectory(nmol, int(fos.max()) + 1, seed=1)
+    with cg.Engine(p, xyz.shape[1]) as eng:
+        ref = eng.run(xyz, box, fos)
+        L, g = eng.loss_grad(xyz, box, fos, 1.01 * ref["ls_ir"], 0.99 * ref["ls_vv"])
+        print(f"grad nmol {nmol}: loss {L:.4e}", eng.stats(), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -68,11 +81,17 @@ def main() -> None:
     r.add_argument("--precision", default="fp32")
     for opt in ("propagate-vectors", "share-frames", "refine-eigen"):
         r.add_argument("--" + opt, type=int, default=0)
+    gr = sub.add_parser("grad")
+    gr.add_argument("--nmol", type=int, default=256)
+    gr.add_argument("--nsamples", type=int, default=2)
+    gr.add_argument("--ntcf", type=int, default=32)
     a = ap.parse_args()
     if a.cmd == "eigh":
         eigh(a.nmol, [int(x) for x in a.batch.split(",")])
     elif a.cmd == "prop":
         prop(a.n, a.nprop, a.precision)
+    elif a.cmd == "grad":
+        grad(a.nmol, a.nsamples, a.ntcf)
     else:
         run(a.nmol, a.nsamples, a.ntcf, a.precision, propagate_vectors=a.propagate_vectors,
             share_frames=a.share_frames, refine_eigen=a.refine_eigen)

@@ -89,3 +89,31 @@ def test_autograd_wrapper_and_gpu_central_difference(lib):
         hq = float(np.float32(th0[q] + h)) - float(np.float32(th0[q] - h))   # the step as stored in float32
         fd = (vals[0] - vals[1]) / hq
         assert abs(fd - g[q]) <= 2e-2 * abs(g[q]), (A.THETA_NAMES[q], fd, g[q])
+
+
+def test_loss_grad_config_size(lib):
+    """The differentiation configuration itself -- 256 molecules (512 chromophores), 4 origins
+    x 200 points, targets from map coefficients perturbed by seeded +-2% noise -- against the
+    loss and the FP64 adjoint gradient stored by tests/golden/make_configs.py."""
+    import os
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import make_configs as MC
+    path = os.path.join(GOLDEN, "diff_256h2o.npz")
+    if not os.path.exists(path):
+        pytest.skip("diff_256h2o.npz not generated (tests/golden/make_configs.py)")
+    z = np.load(path)
+    xyz, box, fos = MC.diff_frames(lib.synth_trajectory)
+    assert np.array_equal(fos, z["frame_table"])
+    q = {k: MC.DIFF_PRM[k] for k in ("ntcfpoints", "nsamples", "sampleEvery", "omegaStep", "nzeros", "map", "dt",
+                                     "t1", "avef", "beginTime", "omegaStart", "omegaStop")}
+    p = lib.default_params(model="tip4p2005", species="H2O", **q)
+    th0 = z["theta0"]
+    with lib.Engine(p, xyz.shape[1]) as eng:
+        np.testing.assert_array_equal(eng.get_coeffs(), th0.astype(np.float32))
+        L, g = eng.loss_grad(xyz, box, fos.astype(np.int32), z["target_ir"], z["target_vv"])
+    Lref = float(z["loss"])
+    assert abs(L - Lref) <= BAR * Lref, (L, Lref)
+    err = _close(g, z["grad"], th0, "FP64 adjoint, 256 H2O 4 x 200")
+    print(f"config-size gradient: worst theta_i dL/dtheta_i error {err:.2e} of the largest")

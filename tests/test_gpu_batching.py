@@ -100,3 +100,41 @@ def test_autotuner_tile_shapes_agree(lib):
     with lib.Engine(p_on, xyz.shape[1]) as eng:
         on = eng.run(xyz, box, fos)
     _same(on, off, 1e-6, "autotuned")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_run_multi_config_sizes_against_oracle(lib, precision):
+    """The batching configuration's sizes -- 128, 216, 343 and 512 molecules, two seeded
+    trajectories each, 200 points -- in one cir_run_multi job, each trajectory against its
+    FP64 oracle spectra (tests/golden/make_configs.py): the plain form within 1e-4, the
+    split-BF16 form within 1e-3 per spectrum."""
+    import os
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import make_configs as MC
+    path = os.path.join(GOLDEN, "batching_2traj.npz")
+    if not os.path.exists(path):
+        pytest.skip("batching_2traj.npz not generated (tests/golden/make_configs.py)")
+    z = np.load(path)
+    q = {k: MC.BATCH_PRM[k] for k in ("ntcfpoints", "nsamples", "sampleEvery", "omegaStep", "nzeros", "map", "dt",
+                                      "t1", "avef", "beginTime", "omegaStart", "omegaStop")}
+    p = lib.default_params(model="tip4p2005", species="H2O", precision=precision, **q)
+    trajs, names = [], []
+    for nmol in MC.BATCH_SIZES:
+        for t in range(MC.BATCH_TRAJ):
+            xyz, box = lib.synth_trajectory(nmol, MC.BATCH_PRM["ntcfpoints"], seed=MC.batch_seed(nmol, t))
+            trajs.append((xyz, box, None))
+            names.append(f"n{nmol}_t{t}_")
+    with lib.Engine(p, 4 * MC.BATCH_SIZES[0]) as eng:
+        outs = eng.run_multi(trajs)
+    tol = SPEC_TOL if precision == "fp32" else 1e-3
+    worst = 0.0
+    for out, key in zip(outs, names):
+        ref = MC.batching_spectra(z, key)
+        for k in KEYS:
+            e = O.rel_l2(out[k], ref[k])
+            worst = max(worst, e)
+            assert e < tol, (key, k, e)
+        assert out["bins_out_of_range"] == int(z[key + "oor"])
+    print(f"batching config sizes {precision}: worst spectrum error {worst:.2e}")

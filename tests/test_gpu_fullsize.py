@@ -19,7 +19,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, ROOT
+from conftest import GOLDEN
 from oracle import oracle as O
 
 sys.path.insert(0, GOLDEN)
@@ -37,7 +37,10 @@ _CACHE = {}
 def _case(lib, nmol):
     """(oracle parameters, oracle result, positions, box, frame table) of a fixture."""
     if nmol not in _CACHE:
-        prm, acc, nm, seed, fos = MF.load(os.path.join(GOLDEN, MF.CONFIGS[nmol]["name"] + ".npz"))
+        path = os.path.join(GOLDEN, MF.CONFIGS[nmol]["name"] + ".npz")
+        if not os.path.exists(path):
+            pytest.skip(f"{path} not generated (tests/golden/make_fullsize.py)")
+        prm, acc, nm, seed, fos = MF.load(path)
         ref = O.finish(prm, acc)
         xyz, box = lib.synth_trajectory(nm, int(fos.max()) + 1, seed=seed)
         _CACHE[nmol] = (prm, ref, xyz, box, np.asarray(fos, np.int32))
