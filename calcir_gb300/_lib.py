@@ -71,6 +71,7 @@ class Stats(C.Structure):
         ("kernel_launches", C.c_longlong), ("eig_sweeps", C.c_longlong), ("frame_steps", C.c_longlong),
         ("ms_build", C.c_double), ("ms_eig", C.c_double), ("ms_prop", C.c_double), ("ms_tcf", C.c_double),
         ("ms_tridiag", C.c_double), ("eig_matrices", C.c_longlong),
+        ("tuned_split_tile", C.c_int), ("tuned_tridiag_blocks", C.c_int),
     ]
 
 

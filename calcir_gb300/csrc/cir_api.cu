@@ -81,6 +81,11 @@ struct cir_ctx {
     cudaEvent_t ev[8];
     CirMaps maps;
     std::map<GemmShape, int> gemm_tile;   // autotuner: SIMT tile shape per product shape
+    // autotuner, mixed forms: tile width of each split-BF16 product shape (M, N, K, batch,
+    // epilogue, output form, fused contraction) and tridiagonalisation blocks per SM per order
+    std::map<std::tuple<int, int, int, int, int, int, int>, int> split_tile;
+    std::map<int, int> tq_blocks;
+    int last_split_tile = 0, last_tq_blocks = 0;
     std::vector<GraphEntry> graphs;       // captured step loops, most recent last
 };
 
@@ -272,6 +277,8 @@ extern "C" int cir_synchronize(cir_ctx *c) {
 extern "C" int cir_get_stats(cir_ctx *c, cir_stats *s) {
     if (!c || !s) return cir_fail(CIR_ERR_ARG, "cir_get_stats: null pointer");
     *s = c->stats;
+    s->tuned_split_tile = c->last_split_tile;
+    s->tuned_tridiag_blocks = c->last_tq_blocks;
     return CIR_OK;
 }
 
@@ -475,6 +482,124 @@ static int autotune_gemm(cir_ctx *c, const GemmArgs &g, int batch) {
     c->gemm_tile[gemm_shape(g, batch)] = pick;
     if (c->p.verbose) printf("autotune: GEMM %d x %d x %d (batch %d): %s tiles\n", g.M, g.N, g.K, batch,
                              pick == CIR_GEMM_TILE_64 ? "64 x 64" : "128 x 128");
+    return CIR_OK;
+}
+
+static std::tuple<int, int, int, int, int, int, int> split_shape(const SplitGemmArgs &g, int batch) {
+    return std::make_tuple(g.M, g.N, g.K, batch, g.epilogue, g.out_mode, g.tcf_out != nullptr ? 1 : 0);
+}
+
+// The tile width the autotuner chose for a split-BF16 product shape (0: the launcher's own).
+static int tuned_split(cir_ctx *c, const SplitGemmArgs &g, int batch) {
+    auto it = c->split_tile.find(split_shape(g, batch));
+    return it == c->split_tile.end() ? 0 : it->second;
+}
+
+// Autotuner for the tensor-core form: times the persistent split-BF16 GEMM with 128 x 128
+// and 128 x 256 tiles once per product shape, on zeroed scratch operands of the same sizes
+// and strides (the caller's data untouched; the fused contraction's sums go to scratch),
+// and keeps the faster.  Both widths accumulate every output in the same order, so the
+// choice changes speed only.  Must run outside stream capture.
+static int autotune_split(cir_ctx *c, const SplitGemmArgs &g, int batch) {
+    if (!c->p.autotune || c->split_tile.count(split_shape(g, batch))) return CIR_OK;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t a_b = al((size_t)g.sA * batch * 2), b_b = al((size_t)g.sB * batch * 2),
+                 c_b = al((size_t)g.sC * batch * (g.out_mode == 2 ? 4 : 2)), d_b = g.epilogue == 2 ? al((size_t)g.sD * batch * 2) : 0,
+                 w_b = g.epilogue == 1 ? al((size_t)g.wstride * batch * 4 + 64) : 0,
+                 m_b = g.tcf_out ? al(((size_t)g.tcf_sm0 + g.tcf_smt) * batch * 4 + 64) : 0,
+                 o_b = g.tcf_out ? al((size_t)g.tcf_sout * batch * 8 + 64) : 0;
+    const size_t tot = 2 * a_b + 2 * b_b + 2 * c_b + 2 * d_b + w_b + m_b + o_b;
+    CK(c->buf[B_TUNE].ensure(tot));
+    CK(cudaMemsetAsync(c->buf[B_TUNE].p, 0, tot, c->stream));
+    unsigned char *q = c->buf[B_TUNE].as<unsigned char>();
+    auto take = [&](size_t b) { unsigned char *r = q; q += b; return r; };
+    SplitGemmArgs t = g;
+    t.Ahi = reinterpret_cast<__nv_bfloat16 *>(take(a_b)); t.Alo = reinterpret_cast<__nv_bfloat16 *>(take(a_b));
+    t.Bhi = reinterpret_cast<__nv_bfloat16 *>(take(b_b)); t.Blo = reinterpret_cast<__nv_bfloat16 *>(take(b_b));
+    unsigned char *c0 = take(c_b), *c1 = take(c_b);
+    t.Chi = reinterpret_cast<__nv_bfloat16 *>(c0); t.Clo = reinterpret_cast<__nv_bfloat16 *>(c1);
+    t.Cf = reinterpret_cast<float *>(c0);
+    if (d_b) { t.Dhi = reinterpret_cast<__nv_bfloat16 *>(take(d_b)); t.Dlo = reinterpret_cast<__nv_bfloat16 *>(take(d_b)); }
+    if (w_b) t.w = reinterpret_cast<float *>(take(w_b));
+    if (m_b) {
+        float *m = reinterpret_cast<float *>(take(m_b));
+        t.tcf_m0 = m;
+        t.tcf_mt = m + (size_t)g.tcf_sm0 * batch;
+    }
+    if (o_b) t.tcf_out = reinterpret_cast<double *>(take(o_b));
+    t.test_stall = 0;
+    float best = 1e30f;
+    int pick = 0;
+    for (int tile : {128, 256}) {
+        t.tile_n = tile;
+        CK(cir_launch_split_gemm(t, batch, c->stream, nullptr));   // warm-up
+        CK(cudaEventRecord(c->ev[6], c->stream));
+        for (int r = 0; r < 3; r++) CK(cir_launch_split_gemm(t, batch, c->stream, nullptr));
+        CK(cudaEventRecord(c->ev[7], c->stream));
+        CK(cudaEventSynchronize(c->ev[7]));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
+        if (ms < best) { best = ms; pick = tile; }
+    }
+    c->buf[B_TUNE].release();
+    c->split_tile[split_shape(g, batch)] = pick;
+    c->last_split_tile = pick;
+    if (c->p.verbose) printf("autotune: split-BF16 GEMM %d x %d x %d (batch %d): 128 x %d tiles\n", g.M, g.N, g.K,
+                             batch, pick);
+    return CIR_OK;
+}
+
+// Autotuner for the tridiagonalisation: blocks per SM (its own occupancy or one less),
+// timed once per order on copies of up to 6 waves of the caller's first matrices, restored
+// before every trial; keeps the faster per matrix.  Must run outside stream capture.
+static int autotune_tridiag(cir_ctx *c, const EighArgs &e, int nmat) {
+    if (!c->p.autotune || c->tq_blocks.count(e.n)) return CIR_OK;
+    const int def = cir_tridiag_blocks(e.n);
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int sample = std::min(nmat, 6 * sms);
+    if (def < 2 || sample < 2 * sms) {   // too few matrices to tell the variants apart
+        c->tq_blocks[e.n] = 0;
+        return CIR_OK;
+    }
+    const size_t mb = (size_t)e.mstride * 4;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t a_b = al(sample * mb), de_b = al(sample * cir_eigh_de_bytes(e.ld)), st_b = al((size_t)sample * 4);
+    CK(c->buf[B_TUNE].ensure(3 * a_b + de_b + st_b));
+    unsigned char *q = c->buf[B_TUNE].as<unsigned char>();
+    float *orig = reinterpret_cast<float *>(q), *work = reinterpret_cast<float *>(q + a_b);
+    EighArgs t;
+    memset(&t, 0, sizeof t);
+    t.A = work;
+    t.Z = reinterpret_cast<float *>(q + 2 * a_b);
+    t.DE = reinterpret_cast<float *>(q + 3 * a_b);
+    t.status = reinterpret_cast<int *>(q + 3 * a_b + de_b);
+    t.mstride = e.mstride;
+    t.n = e.n;
+    t.ld = e.ld;
+    CK(cudaMemcpyAsync(orig, e.A, sample * mb, cudaMemcpyDeviceToDevice, c->stream));
+    float best = 1e30f;
+    int pick = 0;
+    for (int blocks : {def, def - 1}) {
+        t.tq_blocks = blocks;
+        float ms_best = 1e30f;
+        for (int r = 0; r < 2; r++) {
+            CK(cudaMemcpyAsync(work, orig, sample * mb, cudaMemcpyDeviceToDevice, c->stream));
+            CK(cudaEventRecord(c->ev[6], c->stream));
+            CK(cir_launch_tridiag(t, sample, c->stream));
+            CK(cudaEventRecord(c->ev[7], c->stream));
+            CK(cudaEventSynchronize(c->ev[7]));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]));
+            ms_best = std::min(ms_best, ms);
+        }
+        if (ms_best < best) { best = ms_best; pick = blocks; }
+    }
+    c->buf[B_TUNE].release();
+    c->tq_blocks[e.n] = pick == def ? 0 : pick;
+    c->last_tq_blocks = pick;
+    if (c->p.verbose) printf("autotune: tridiagonalisation of order %d: %d blocks per SM\n", e.n, pick);
     return CIR_OK;
 }
 
@@ -765,6 +890,25 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         if ((rc = autotune_gemm(c, g2, St))) return rc;
     }
     const int tile1 = tuned_tile(c, g1, St), tile2 = tuned_tile(c, g2, St);
+    // the split-BF16 products' tile widths (the shapes and strides of the step loop's two
+    // products; the autotuner runs them on scratch operands)
+    int stile1 = 0, stile2 = 0;
+    if (split) {
+        SplitGemmArgs r1{};
+        r1.lda = r1.ldb = r1.ldc = ldh; r1.sA = vs_el; r1.sB = r1.sC = fs_el;
+        r1.M = n; r1.N = 2 * n; r1.K = n; r1.epilogue = 1; r1.wstride = std::min(kn, K) * ld;
+        r1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
+        r1.err = c->buf[B_ERR].as<int>();
+        SplitGemmArgs r2 = r1;
+        r2.epilogue = 0;
+        r2.tcf_sm0 = 9LL * ld; r2.tcf_smt = (long long)std::min(kn, K) * 9 * ld; r2.tcf_ldv = ld;
+        r2.tcf_sout = (long long)K * 6;
+        r2.tcf_out = tcf;   // marks the fused form; the autotuner substitutes scratch
+        if ((rc = autotune_split(c, r1, St))) return rc;
+        if ((rc = autotune_split(c, r2, St))) return rc;
+        stile1 = tuned_split(c, r1, St);
+        stile2 = tuned_split(c, r2, St);
+    }
 
     CK(cudaEventRecord(ev[0], c->stream));
     for (int k0 = 0; k0 < K; k0 += kn) {
@@ -860,6 +1004,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
             CK(cudaMemsetAsync(c->buf[B_PROF].p, 0, (size_t)nmat * CIR_EIG_PROF_SLOTS * 8, c->stream));
             e.phase_ns = c->buf[B_PROF].as<unsigned long long>();
         }
+        if (k0 == 0 && (rc = autotune_tridiag(c, e, nmat))) return rc;
+        if (c->tq_blocks.count(n)) e.tq_blocks = c->tq_blocks[n];
         if ((rc = setup_refine(c, e, nmat))) return rc;
         CK(cir_launch_eigh(e, nmat, c->stream, &launches));
         c->stats.eig_matrices += nmat;
@@ -924,6 +1070,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                     s2.tcf_m0 = M0; s2.tcf_sm0 = 9LL * ld;
                     s2.tcf_mt = M + mk * 9 * ld; s2.tcf_smt = (long long)dlt * 9 * ld; s2.tcf_ldv = ld;
                     s2.tcf_out = tcf + (size_t)k * 6; s2.tcf_sout = (long long)K * 6;
+                    s1.tile_n = stile1;
+                    s2.tile_n = stile2;
                     CK(cir_launch_split_gemm(s1, St, c->stream, &nl));
                     CK(cir_launch_split_gemm(s2, St, c->stream, &nl));
                     continue;
@@ -956,7 +1104,7 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         };
         if (p.cuda_graphs) {
             std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2, vs, fs);
-            key.insert(key.end(), {(long long)vectors, (long long)base0, (long long)dlt,
+            key.insert(key.end(), {(long long)vectors, (long long)base0, (long long)dlt, (long long)stile1, (long long)stile2,
                                    (long long)(uintptr_t)c->buf[B_PSI].p, (long long)(uintptr_t)c->buf[B_LAM].p});
             GraphEntry *ge = nullptr;
             for (auto &x : c->graphs)

@@ -108,11 +108,21 @@ struct EighArgs {
     // fault drills (tests only, 0 = off): the split-BF16 GEMMs' stall (SplitGemmArgs::test_stall)
     // and a cap on the QR sweeps of each divide-and-conquer leaf
     int test_stall, test_sweep_cap;
+    // set by the launcher: 1 walks the tiles of the tridiagonalisation's matrix-vector
+    // products in reverse order on alternate columns (CIR_TQ_ORDER=0 keeps one order)
+    int tq_order;
+    // thread blocks of the tridiagonalisation per SM: 0 the kernel's own occupancy, or a
+    // smaller count enforced through its shared-memory request (the autotuner's choice)
+    int tq_blocks;
 };
 
 // kernel launchers (return cudaError_t of the launch)
 cudaError_t cir_launch_build(const BuildArgs &a, int nframes, cudaStream_t s, int *launches);
 cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches);
+// the tridiagonalisation kernel alone (phase 1 of cir_launch_eigh), for the autotuner
+cudaError_t cir_launch_tridiag(const EighArgs &a, int nmat, cudaStream_t s);
+// thread blocks per SM the tridiagonalisation of order n runs with by default
+int cir_tridiag_blocks(int n);
 size_t cir_eigh_rot_bytes(int n);
 size_t cir_eigh_de_bytes(int ld);
 size_t cir_dc_bytes(int n, int ld);
@@ -195,6 +205,7 @@ struct SplitGemmArgs {
     int bz0;              // batch entry of blockIdx.z == 0 (set by the launcher when it splits a batch)
     int test_stall;       // fault drill (tests only): 1 withholds the first tile's completion and
                           // shortens the pipeline waits, so that they run out and raise err
+    int tile_n;           // tile width: 0 picks by shape; 128 or 256 forces it (the autotuner's choice)
 };
 size_t cir_split_ld(int n);   // leading dimension of the split operands (n rounded up to 8)
 cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches);

@@ -504,7 +504,8 @@ __device__ void trail_update(float *__restrict__ A, const float *__restrict__ Wb
 // per warp), pv (4 x TB_NB) and stage (aliasing ywall) are shared memory.
 template <int NT, int NMAX>
 __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, int n, int ld, float *d, float *e,
-                                float *tau, float *x, float *ywall, float *pv, float *red, unsigned long long *pt) {
+                                float *tau, float *x, float *ywall, float *pv, float *red, unsigned long long *pt,
+                                int tq_order) {
     constexpr int NW = NT / 32;
     constexpr int RW = (NMAX + NT - 1) / NT;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -571,20 +572,33 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
             for (int i = 32 * j0 + lane; i < n32; i += 32) ywp[i] = 0.f;
             __syncthreads();
             mark(13);
-            // (c) y = A22 v on the panel-start trailing block, plus t1 = W^T v, t2 = V^T v
+            // (c) y = A22 v on the panel-start trailing block, plus t1 = W^T v, t2 = V^T v.
+            // Within a panel consecutive columns read the same tiles (A is not updated until the
+            // panel ends), so alternate columns walk them in opposite orders: a column starts on
+            // the tiles the previous column (or the trailing update, for a panel's first column)
+            // read last, which are the ones most likely still in L2.
             {
                 const int tt = tn - j0;
                 const int ntiles = tt * (tt + 1) / 2;
-                int Ii = 0, Jj = warp;       // row-major enumeration of the lower triangle
-                while (Jj > Ii) { Jj -= Ii + 1; Ii++; }
+                const bool rev = tq_order && (kk & 1) == 0;
+                // tile of position L of the row-major enumeration of the lower triangle
+                auto tile_of = [&](int L, int &Ii, int &Jj) {
+                    int i = (int)((sqrtf(8.f * (float)L + 1.f) - 1.f) * 0.5f);
+                    while (i * (i + 1) / 2 > L) i--;
+                    while ((i + 1) * (i + 2) / 2 <= L) i++;
+                    Ii = i;
+                    Jj = L - i * (i + 1) / 2;
+                };
                 for (int q = warp; q < ntiles; q += NW) {
-                    const int I = j0 + Ii, J = j0 + Jj;
-                    Jj += NW;                // this warp's next tile, whose lines are requested
-                    while (Jj > Ii) { Jj -= Ii + 1; Ii++; }   // into L2 before this one is read
-                    if (q + NW < ntiles) {
-                        const int c = 32 * (j0 + Jj) + lane;
-                        if (c < n) prefetch_l2(A + (size_t)c * ld + 32 * (j0 + Ii));
+                    int Ii, Jj;
+                    tile_of(rev ? ntiles - 1 - q : q, Ii, Jj);
+                    if (q + NW < ntiles) {   // this warp's next tile: its lines are requested into L2
+                        int In, Jn;
+                        tile_of(rev ? ntiles - 1 - (q + NW) : q + NW, In, Jn);
+                        const int c = 32 * (j0 + Jn) + lane;
+                        if (c < n) prefetch_l2(A + (size_t)c * ld + 32 * (j0 + In));
                     }
+                    const int I = j0 + Ii, J = j0 + Jj;
                     if (I == J || 32 * I + 32 > n) symv_tile<true>(A, ld, n, I, J, x, ywp, lane);
                     else symv_tile<false>(A, ld, n, I, J, x, ywp, lane);
                 }
@@ -719,7 +733,7 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
         // W of the current panel lives in Z, which phase 2 overwrites
         const int n32 = (n + 31) & ~31;
         const int yws = max(n32 * NW, 2 * tb_stage(NT));
-        tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red, pt);
+        tridiag_blocked<NT, NMAX>(A, Z, n, ld, d, e, tau, U, U + n32, U + n32 + yws, red, pt, a.tq_order);
     } else {
         float *vp = U, *wp = U + n4, *vc = U + 2 * n4, *wc = U + 3 * n4;
         // the first column reads vp / wp (scaled by zero) before any update has written them:
@@ -1259,7 +1273,26 @@ cudaError_t launch_tq(const EighArgs &a, int nmat, cudaStream_t s) {
     const size_t smem = tq_smem_bytes(a.n, NT, BLK);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<nmat, NT, smem, s>>>(a);
+    static const int order = [] {
+        const char *v = getenv("CIR_TQ_ORDER");
+        return v ? atoi(v) : 1;
+    }();
+    EighArgs b = a;
+    b.tq_order = order;
+    size_t req = smem;
+    if (a.tq_blocks > 0 && a.tq_blocks < MINB) {
+        // fewer blocks per SM: ask for enough shared memory that only tq_blocks fit
+        int dev = 0, per_sm = 0, reserved = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+            return e;
+        const size_t want = (size_t)per_sm / (a.tq_blocks + 1) - (size_t)reserved + 1024;
+        if (want > req) req = want;
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)req)) != cudaSuccess)
+            return e;
+    }
+    kern<<<nmat, NT, req, s>>>(b);
     return cudaGetLastError();
 }
 
@@ -1293,17 +1326,22 @@ size_t cir_eigh_de_bytes(int ld) { return sizeof(float) * 3 * (size_t)ld; }
 
 int cir_eigh_max_n() { return 2048; }
 
+int cir_tridiag_blocks(int n) { return n <= 256 ? 4 : (n <= 1024 ? 3 : 2); }
+
+cudaError_t cir_launch_tridiag(const EighArgs &a, int nmat, cudaStream_t s) {
+    if (a.n <= 256) return launch_tq<128, 256, 4, false>(a, nmat, s);
+    if (a.n <= 512) return launch_tq<256, 512, 3, true>(a, nmat, s);
+    if (a.n <= 1024) return launch_tq<256, 1024, 3, true>(a, nmat, s);
+    return launch_tq<256, 2048, 2, true>(a, nmat, s);
+}
+
 cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *launches) {
     if (a.n < 1 || a.n > cir_eigh_max_n() || nmat < 1 || nmat > 65535 || (a.ld & 3) || a.ld < a.n)
         return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.DE ||
         (!a.rot && !a.DC) || (a.DC && (reinterpret_cast<uintptr_t>(a.DC) & 15)))
         return cudaErrorInvalidValue;
-    cudaError_t e;
-    if (a.n <= 256) e = launch_tq<128, 256, 4, false>(a, nmat, s);
-    else if (a.n <= 512) e = launch_tq<256, 512, 3, true>(a, nmat, s);
-    else if (a.n <= 1024) e = launch_tq<256, 1024, 3, true>(a, nmat, s);
-    else e = launch_tq<256, 2048, 2, true>(a, nmat, s);
+    cudaError_t e = cir_launch_tridiag(a, nmat, s);
     if (e != cudaSuccess) return e;
     if (a.tq_done && (e = cudaEventRecord(a.tq_done, s)) != cudaSuccess) return e;
     if (launches) *launches += 1;

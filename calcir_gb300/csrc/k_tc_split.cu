@@ -787,7 +787,9 @@ cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_
     const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
     // 128 x 256 tiles for the wide products (the propagation) and the back-transform updates
     // (C = D - A B): a quarter less operand traffic per flop
-    const int qn = ((g.N >= 1024 && g.K > 4 * QK) || (g.epilogue == 2 && g.N >= 256)) ? 256 : 128;
+    const int qn = (g.tile_n == 128 || g.tile_n == 256)
+                       ? g.tile_n
+                       : (((g.N >= 1024 && g.K > 4 * QK) || (g.epilogue == 2 && g.N >= 256)) ? 256 : 128);
     if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK, QM) ||
         !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch, QK, QM) ||
         !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) ||

@@ -129,6 +129,10 @@ typedef struct cir_stats {
     double    ms_build, ms_eig, ms_prop, ms_tcf;   /* device time per stage of cir_run*  */
     double    ms_tridiag;               /* of ms_eig: the tridiagonalisation kernel       */
     long long eig_matrices;             /* Hamiltonians built and diagonalised by cir_run* */
+    int       tuned_split_tile;         /* autotuner (autotune 1): tile width (128 or 256) it chose
+                                           for the last tuned tensor-core propagation product, 0 none */
+    int       tuned_tridiag_blocks;     /* autotuner: tridiagonalisation blocks per SM it chose for
+                                           the last tuned order, 0 none                       */
 } cir_stats;
 
 /* Parameters for the seeded synthetic water-box generator (replaces the .xtc source). */

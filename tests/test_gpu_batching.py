@@ -138,3 +138,26 @@ def test_run_multi_config_sizes_against_oracle(lib, precision):
             assert e < tol, (key, k, e)
         assert out["bins_out_of_range"] == int(z[key + "oor"])
     print(f"batching config sizes {precision}: worst spectrum error {worst:.2e}")
+
+
+def test_autotuner_tensor_core_forms_agree(lib):
+    """In the split-BF16 form the autotuner also picks the propagation products' tile width
+    (128 x 128 or 128 x 256 on the persistent tcgen05 GEMM) and the tridiagonalisation's
+    thread blocks per SM; both change speed only, so the tuned run equals the untuned one."""
+    keys = dict(model="tip4p2005", species="H2O", ntcfpoints=160, nsamples=2, sampleEvery=0.05, omegaStart=1000,
+                omegaStop=5000, omegaStep=1, nzeros=600, precision="bf16x3")
+    p_on = lib.default_params(**keys)
+    p_off = lib.default_params(autotune=0, **keys)
+    fos = lib.frame_table(p_on, 0.010)
+    xyz, box = lib.synth_trajectory(64, int(fos.max()) + 1, seed=21)
+    with lib.Engine(p_off, xyz.shape[1]) as eng:
+        off = eng.run(xyz, box, fos)
+        st_off = eng.stats()
+    with lib.Engine(p_on, xyz.shape[1]) as eng:
+        on = eng.run(xyz, box, fos)
+        st = eng.stats()
+    assert st_off["tuned_split_tile"] == 0 and st_off["tuned_tridiag_blocks"] == 0
+    assert st["tuned_split_tile"] in (128, 256), st
+    assert st["tuned_tridiag_blocks"] in (3, 4), st      # order 128: four blocks per SM by default
+    print("autotuner picked", st["tuned_split_tile"], "wide tiles,", st["tuned_tridiag_blocks"], "blocks per SM")
+    _same(on, off, 1e-6, "autotuned tensor-core form")
