@@ -6,8 +6,18 @@
 #include <cuda_bf16.h>
 #include "cir_internal.h"
 
-// minImage (calcIR.cu:1459-1463): dx - L*round(dx/L), round half away from zero.
-__device__ __forceinline__ float cir_mi(float dx, float L) { return dx - L * roundf(dx / L); }
+// minImage (calcIR.cu:1459-1463): dx - L*round(dx/L), round half away from zero, evaluated
+// as the reference's float expression is, one rounding per operation (no fused multiply-add),
+// so that the image chosen at the box's half-width rounds as the reference rounds it.
+__device__ __forceinline__ float cir_mi(float dx, float L) {
+    return __fsub_rn(dx, __fmul_rn(L, roundf(__fdiv_rn(dx, L))));
+}
+// mag3 (calcIR.cu:1464-1476): sqrt(x*x + y*y + z*z) with the reference's order of operations
+// and one rounding each; the field's cutoff test compares it with 0.7831 nm, a discontinuous
+// decision that a contracted evaluation would take differently for pairs within an ulp of it.
+__device__ __forceinline__ float cir_mag3(float x, float y, float z) {
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+}
 
 __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

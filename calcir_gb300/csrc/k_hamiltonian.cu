@@ -67,8 +67,7 @@ __global__ void __launch_bounds__(CHROM_THREADS) k_chromophore(BuildArgs a) {
             if (t0 + j == n) continue;
             const float *mo = sm_mol[j];
             const float dx = cir_mi(mo[0] - hx, bx), dy = cir_mi(mo[1] - hy, by), dz = cir_mi(mo[2] - hz, bz);
-            const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-            if (r > CIR_CUTOFF) continue;
+            if (cir_mag3(dx, dy, dz) > CIR_CUTOFF) continue;   // calcIR.cu:1106-1113
             #pragma unroll
             for (int s = 0; s < 3; s++) {
                 float sx, sy, sz, q;
