@@ -19,7 +19,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <memory>
 #include <tuple>
 #include <algorithm>
 #include <vector>
@@ -87,6 +89,8 @@ struct cir_ctx {
     std::map<int, int> tq_blocks;
     int last_split_tile = 0, last_tq_blocks = 0;
     std::vector<GraphEntry> graphs;       // captured step loops, most recent last
+    // device buffers of the second and later groups of a joint cir_run_multi job
+    std::vector<std::unique_ptr<DevBuf[]>> gbuf;
 };
 
 #define CK(call)                                                                                        \
@@ -256,6 +260,8 @@ extern "C" int cir_destroy(cir_ctx *c) {
     for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
     c->graphs.clear();
     for (auto &b : c->buf) b.release();
+    for (auto &gb : c->gbuf)
+        for (int i = 0; i < B_COUNT; i++) gb[i].release();
     for (auto &e : c->ev) cudaEventDestroy(e);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -799,127 +805,176 @@ static std::vector<long long> step_key(const Group &g, int St, int K, int k0, in
 static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long long sV, const float *w, long long sw,
                          float dt, float *x, float *tmp, int &launches);
 
-// The frame-steps of one group: ntraj trajectories of one size, nsamples origins each.
-// dxyz / dbox hold all the group's frames on the device; fidx[(t*S + s)*K + k] is the frame
-// of step k of origin s of trajectory t.  res[t] receives trajectory t's results.
-static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float *dbox, const std::vector<int> &fidx,
-                     cir_result *res, double *ms_run) {
-    const cir_params &p = c->p;
-    const int S = p.nsamples, K = p.ntcfpoints, n = g.n, ld = g.ld, T = g.ntraj;
-    const int St = S * T;                                    // origins of the group
-    const int nomega = cir_nomega(&p);
-    const long long steps = (long long)St * K;
-
-    // chunk: kn consecutive steps of all St origins per batch
-    const size_t per_step = (size_t)(p.refine_eigen > 0 ? 3 : 2) * n * ld * 4 + cir_dc_bytes(n, ld) +
-                            cir_eigh_de_bytes(ld) + (size_t)(9 + CT_NROW + 1) * ld * 4 + (size_t)g.natoms * 12 + 64;
-    size_t budget = (size_t)64 << 30;
-    size_t freeb = 0, totalb = 0;
-    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
-    int kn = (int)std::max<size_t>(1, budget / (per_step * St));
-    if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / St);
-    kn = std::min(kn, K);
-    kn = std::max(1, std::min(kn, 65535 / std::max(1, St)));   // matrices of a chunk index a grid dimension
-    if (St > 65535) return cir_fail(CIR_ERR_ARG, "%d time origins in one group (at most 65535)", St);
-
-    CK(c->buf[B_FIDX].ensure((size_t)steps * 4));
-    CK(cudaMemcpyAsync(c->buf[B_FIDX].p, fidx.data(), (size_t)steps * 4, cudaMemcpyHostToDevice, c->stream));
-    const int nb = St * kn;
-    const long long mstride = (long long)n * ld;
-    CK(c->buf[B_CXYZ].ensure((size_t)nb * g.natoms * 12));
-    CK(c->buf[B_CBOX].ensure((size_t)nb * 12));
-    CK(c->buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
-    CK(c->buf[B_A].ensure((size_t)nb * mstride * 4));
-    CK(c->buf[B_Z].ensure((size_t)nb * mstride * 4));
-    CK(c->buf[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
-    CK(c->buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
-    CK(c->buf[B_W].ensure((size_t)nb * ld * 4));
-    CK(c->buf[B_M].ensure((size_t)nb * 9 * ld * 4));
-    CK(c->buf[B_STATUS].ensure((size_t)nb * 4));
-    // the split-BF16 form propagates pre-split operands (k_tc_split.cu): per origin the
-    // step's V as Vc and Vr and the transposed F and G, each a hi/lo pair of order ldh
-    const bool vectors = p.propagate_vectors != 0;   // psi = F m(0) instead of F
-    const bool split = !vectors && p.precision == CIR_PREC_BF16X3;
-    const int ldh = (int)cir_split_ld(n);
-    const long long vs_el = (long long)n * ldh, fs_el = (long long)2 * n * ldh;   // elements per origin
-    if (vectors) {
-        CK(c->buf[B_PSI].ensure((size_t)St * n * CIR_PSI_LD * 4));
-        CK(c->buf[B_LAM].ensure((size_t)St * n * CIR_PSI_LD * 4));
-    } else if (split) {
-        CK(c->buf[B_VS].ensure((size_t)4 * St * vs_el * 2));
-        CK(c->buf[B_FS].ensure((size_t)4 * St * fs_el * 2));
-    } else {
-        CK(c->buf[B_F].ensure((size_t)St * n * 2 * ld * 4));
-        CK(c->buf[B_G].ensure((size_t)St * n * 2 * ld * 4));
-    }
-    CK(c->buf[B_M0].ensure((size_t)St * 9 * ld * 4));
-    CK(c->buf[B_TCF].ensure((size_t)steps * 6 * 8));
-    CK(c->buf[B_HCNT].ensure((size_t)T * nomega * 8));
-    CK(c->buf[B_HIPR].ensure((size_t)T * nomega * 8));
-    CK(c->buf[B_HMIPR].ensure((size_t)T * nomega * 8));
-    CK(c->buf[B_OOR].ensure((size_t)T * 8));
-    CK(c->buf[B_SWEEPS].ensure(8));
-    CK(c->buf[B_SW].ensure((size_t)T * nomega * 8));
-    CK(c->buf[B_MU2].ensure((size_t)ld * 4));
-    CK(cudaMemsetAsync(c->buf[B_TCF].p, 0, (size_t)steps * 48, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_HCNT].p, 0, (size_t)T * nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_HIPR].p, 0, (size_t)T * nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_HMIPR].p, 0, (size_t)T * nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_OOR].p, 0, (size_t)T * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_SWEEPS].p, 0, 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_SW].p, 0, (size_t)T * nomega * 8, c->stream));
-    CK(cudaMemsetAsync(c->buf[B_STATUS].p, 0, (size_t)nb * 4, c->stream));
-
-    float *A = c->buf[B_A].as<float>(), *W = c->buf[B_W].as<float>(), *M = c->buf[B_M].as<float>();
-    float *F = c->buf[B_F].as<float>(), *G = c->buf[B_G].as<float>(), *M0 = c->buf[B_M0].as<float>();
-    __nv_bfloat16 *vs = split ? c->buf[B_VS].as<__nv_bfloat16>() : nullptr;
-    __nv_bfloat16 *fs = split ? c->buf[B_FS].as<__nv_bfloat16>() : nullptr;
-    const SplitMat Vc{vs, vs + St * vs_el}, Vr{vs + 2 * St * vs_el, vs + 3 * St * vs_el};
-    const SplitMat Ft{fs, fs + St * fs_el}, Gt{fs + 2 * St * fs_el, fs + 3 * St * fs_el};
-    double *tcf = c->buf[B_TCF].as<double>();
+// One group's job: ntraj trajectories of one size, nsamples origins each, batched through
+// every launch.  dxyz / dbox hold all the group's frames on the device; fidx[(t*S + s)*K + k]
+// is the frame of step k of origin s of trajectory t; res[t] receives trajectory t's results.
+// The job runs in phases -- setup, then per chunk of kn steps the preparation (gather, build,
+// eigensolve, step-0 work) and the step loop, then finish -- so that several groups can run
+// their step loops in joint launches (run_groups_joint).  buf is the job's own device buffers
+// (the context's for a single group).
+struct GroupJob {
+    cir_ctx *c;
+    DevBuf *buf;
+    Group g;
+    const float *dxyz, *dbox;
+    const std::vector<int> &fidx;
+    cir_result *res;
+    const cir_params &p;
+    cudaEvent_t *ev;
+    int S = 0, K = 0, n = 0, ld = 0, T = 0, St = 0, nomega = 0, kn = 0, nb = 0, ldh = 0;
+    long long steps = 0, mstride = 0, vs_el = 0, fs_el = 0;
+    bool vectors = false, split = false;
+    float *A = nullptr, *W = nullptr, *M = nullptr, *F = nullptr, *G = nullptr, *M0 = nullptr;
+    __nv_bfloat16 *vs = nullptr, *fs = nullptr;
+    SplitMat Vc{}, Vr{}, Ft{}, Gt{};
+    double *tcf = nullptr;
+    int tile1 = 0, tile2 = 0, stile1 = 0, stile2 = 0;
     int launches = 0;
-    cudaEvent_t *ev = c->ev;
-    int rc;
+    int k0 = 0, kc = 0, nmat = 0, base0 = 0, dlt = 0;   // the chunk being run
 
-    // the propagation products of this group, tuned before anything is timed or captured
-    GemmArgs g1{}, g2{};
-    g1.M = n; g1.N = 2 * n; g1.K = n; g1.lda = ld; g1.ldb = g1.ldc = 2 * ld; g1.a_colmajor = false; g1.epilogue = 1;
-    g2 = g1; g2.a_colmajor = true; g2.epilogue = 0;
-    if (p.precision == CIR_PREC_FP32) {
-        if ((rc = autotune_gemm(c, g1, St))) return rc;
-        if ((rc = autotune_gemm(c, g2, St))) return rc;
-    }
-    const int tile1 = tuned_tile(c, g1, St), tile2 = tuned_tile(c, g2, St);
-    // the split-BF16 products' tile widths (the shapes and strides of the step loop's two
-    // products; the autotuner runs them on scratch operands)
-    int stile1 = 0, stile2 = 0;
-    if (split) {
-        SplitGemmArgs r1{};
-        r1.lda = r1.ldb = r1.ldc = ldh; r1.sA = vs_el; r1.sB = r1.sC = fs_el;
-        r1.M = n; r1.N = 2 * n; r1.K = n; r1.epilogue = 1; r1.wstride = std::min(kn, K) * ld;
-        r1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
-        r1.err = c->buf[B_ERR].as<int>();
-        SplitGemmArgs r2 = r1;
-        r2.epilogue = 0;
-        r2.tcf_sm0 = 9LL * ld; r2.tcf_smt = (long long)std::min(kn, K) * 9 * ld; r2.tcf_ldv = ld;
-        r2.tcf_sout = (long long)K * 6;
-        r2.tcf_out = tcf;   // marks the fused form; the autotuner substitutes scratch
-        if ((rc = autotune_split(c, r1, St))) return rc;
-        if ((rc = autotune_split(c, r2, St))) return rc;
-        stile1 = tuned_split(c, r1, St);
-        stile2 = tuned_split(c, r2, St);
+    GroupJob(cir_ctx *c_, DevBuf *buf_, const Group &g_, const float *dxyz_, const float *dbox_,
+             const std::vector<int> &fidx_, cir_result *res_)
+        : c(c_), buf(buf_), g(g_), dxyz(dxyz_), dbox(dbox_), fidx(fidx_), res(res_), p(c_->p), ev(c_->ev) {}
+
+    // bytes of device memory one origin-step of a chunk holds
+    static size_t per_step_bytes(const cir_params &p, const Group &g) {
+        return (size_t)(p.refine_eigen > 0 ? 3 : 2) * g.n * g.ld * 4 + cir_dc_bytes(g.n, g.ld) + cir_eigh_de_bytes(g.ld) +
+               (size_t)(9 + CT_NROW + 1) * g.ld * 4 + (size_t)g.natoms * 12 + 64;
     }
 
-    CK(cudaEventRecord(ev[0], c->stream));
-    for (int k0 = 0; k0 < K; k0 += kn) {
-        const int kc = std::min(kn, K - k0);
+    // buffers, zeroed sums, tuned products; kn_set > 0 fixes the chunk length
+    int setup(int kn_set) {
+        S = p.nsamples; K = p.ntcfpoints; n = g.n; ld = g.ld; T = g.ntraj;
+        St = S * T;                                    // origins of the group
+        nomega = cir_nomega(&p);
+        steps = (long long)St * K;
+
+        // chunk: kn consecutive steps of all St origins per batch
+        const size_t per_step = per_step_bytes(p, g);
+        size_t budget = (size_t)64 << 30;
+        size_t freeb = 0, totalb = 0;
+        if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
+        kn = (int)std::max<size_t>(1, budget / (per_step * St));
+        if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / St);
+        if (kn_set > 0) kn = kn_set;   // chosen by the caller for several groups together
+        kn = std::min(kn, K);
+        kn = std::max(1, std::min(kn, 65535 / std::max(1, St)));   // matrices of a chunk index a grid dimension
+        if (St > 65535) return cir_fail(CIR_ERR_ARG, "%d time origins in one group (at most 65535)", St);
+
+        CK(buf[B_FIDX].ensure((size_t)steps * 4));
+        CK(cudaMemcpyAsync(buf[B_FIDX].p, fidx.data(), (size_t)steps * 4, cudaMemcpyHostToDevice, c->stream));
+        nb = St * kn;
+        mstride = (long long)n * ld;
+        CK(buf[B_CXYZ].ensure((size_t)nb * g.natoms * 12));
+        CK(buf[B_CBOX].ensure((size_t)nb * 12));
+        CK(buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
+        CK(buf[B_A].ensure((size_t)nb * mstride * 4));
+        CK(buf[B_Z].ensure((size_t)nb * mstride * 4));
+        CK(buf[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
+        CK(buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
+        CK(buf[B_W].ensure((size_t)nb * ld * 4));
+        CK(buf[B_M].ensure((size_t)nb * 9 * ld * 4));
+        CK(buf[B_STATUS].ensure((size_t)nb * 4));
+        // the split-BF16 form propagates pre-split operands (k_tc_split.cu): per origin the
+        // step's V as Vc and Vr and the transposed F and G, each a hi/lo pair of order ldh
+        vectors = p.propagate_vectors != 0;   // psi = F m(0) instead of F
+        split = !vectors && p.precision == CIR_PREC_BF16X3;
+        ldh = (int)cir_split_ld(n);
+        vs_el = (long long)n * ldh;
+        fs_el = (long long)2 * n * ldh;   // elements per origin
+        if (vectors) {
+            CK(buf[B_PSI].ensure((size_t)St * n * CIR_PSI_LD * 4));
+            CK(buf[B_LAM].ensure((size_t)St * n * CIR_PSI_LD * 4));
+        } else if (split) {
+            CK(buf[B_VS].ensure((size_t)4 * St * vs_el * 2));
+            CK(buf[B_FS].ensure((size_t)4 * St * fs_el * 2));
+        } else {
+            CK(buf[B_F].ensure((size_t)St * n * 2 * ld * 4));
+            CK(buf[B_G].ensure((size_t)St * n * 2 * ld * 4));
+        }
+        CK(buf[B_M0].ensure((size_t)St * 9 * ld * 4));
+        CK(buf[B_TCF].ensure((size_t)steps * 6 * 8));
+        CK(buf[B_HCNT].ensure((size_t)T * nomega * 8));
+        CK(buf[B_HIPR].ensure((size_t)T * nomega * 8));
+        CK(buf[B_HMIPR].ensure((size_t)T * nomega * 8));
+        CK(buf[B_OOR].ensure((size_t)T * 8));
+        CK(buf[B_SWEEPS].ensure(8));
+        CK(buf[B_SW].ensure((size_t)T * nomega * 8));
+        CK(buf[B_MU2].ensure((size_t)ld * 4));
+        CK(cudaMemsetAsync(buf[B_TCF].p, 0, (size_t)steps * 48, c->stream));
+        CK(cudaMemsetAsync(buf[B_HCNT].p, 0, (size_t)T * nomega * 8, c->stream));
+        CK(cudaMemsetAsync(buf[B_HIPR].p, 0, (size_t)T * nomega * 8, c->stream));
+        CK(cudaMemsetAsync(buf[B_HMIPR].p, 0, (size_t)T * nomega * 8, c->stream));
+        CK(cudaMemsetAsync(buf[B_OOR].p, 0, (size_t)T * 8, c->stream));
+        CK(cudaMemsetAsync(buf[B_SWEEPS].p, 0, 8, c->stream));
+        CK(cudaMemsetAsync(buf[B_SW].p, 0, (size_t)T * nomega * 8, c->stream));
+        CK(cudaMemsetAsync(buf[B_STATUS].p, 0, (size_t)nb * 4, c->stream));
+
+        A = buf[B_A].as<float>();
+        W = buf[B_W].as<float>();
+        M = buf[B_M].as<float>();
+        F = buf[B_F].as<float>();
+        G = buf[B_G].as<float>();
+        M0 = buf[B_M0].as<float>();
+        vs = split ? buf[B_VS].as<__nv_bfloat16>() : nullptr;
+        fs = split ? buf[B_FS].as<__nv_bfloat16>() : nullptr;
+        Vc = SplitMat{vs, vs + St * vs_el};
+        Vr = SplitMat{vs + 2 * St * vs_el, vs + 3 * St * vs_el};
+        Ft = SplitMat{fs, fs + St * fs_el};
+        Gt = SplitMat{fs + 2 * St * fs_el, fs + 3 * St * fs_el};
+        tcf = buf[B_TCF].as<double>();
+        launches = 0;
+        int rc;
+
+        // the propagation products of this group, tuned before anything is timed or captured
+        GemmArgs g1{}, g2{};
+        g1.M = n; g1.N = 2 * n; g1.K = n; g1.lda = ld; g1.ldb = g1.ldc = 2 * ld; g1.a_colmajor = false; g1.epilogue = 1;
+        g2 = g1; g2.a_colmajor = true; g2.epilogue = 0;
+        if (p.precision == CIR_PREC_FP32) {
+            if ((rc = autotune_gemm(c, g1, St))) return rc;
+            if ((rc = autotune_gemm(c, g2, St))) return rc;
+        }
+        tile1 = tuned_tile(c, g1, St);
+        tile2 = tuned_tile(c, g2, St);
+        // the split-BF16 products' tile widths (the shapes and strides of the step loop's two
+        // products; the autotuner runs them on scratch operands)
+        stile1 = stile2 = 0;
+        if (split) {
+            SplitGemmArgs r1{};
+            r1.lda = r1.ldb = r1.ldc = ldh; r1.sA = vs_el; r1.sB = r1.sC = fs_el;
+            r1.M = n; r1.N = 2 * n; r1.K = n; r1.epilogue = 1; r1.wstride = std::min(kn, K) * ld;
+            r1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
+            r1.err = c->buf[B_ERR].as<int>();
+            SplitGemmArgs r2 = r1;
+            r2.epilogue = 0;
+            r2.tcf_sm0 = 9LL * ld; r2.tcf_smt = (long long)std::min(kn, K) * 9 * ld; r2.tcf_ldv = ld;
+            r2.tcf_sout = (long long)K * 6;
+            r2.tcf_out = tcf;   // marks the fused form; the autotuner substitutes scratch
+            if ((rc = autotune_split(c, r1, St))) return rc;
+            if ((rc = autotune_split(c, r2, St))) return rc;
+            stile1 = tuned_split(c, r1, St);
+            stile2 = tuned_split(c, r2, St);
+        }
+        return CIR_OK;
+    }
+
+    // the chunk of steps k0_ .. k0_ + kc_ - 1: frames gathered, Hamiltonians built and
+    // diagonalised, the distributions binned; at step 0 the spectral density and F = I.
+    // Records ev[1] (start), ev[2] (built), ev[5] (tridiagonalised), ev[3] (done); with
+    // account, waits for ev[3] and adds the build and eigensolver times to the stats.
+    int prepare(int k0_, int kc_, bool account) {
+        k0 = k0_;
+        kc = kc_;
+        int rc;
         const int nbc = St * kc;
         // Matrix of origin s at step k0 + kk: base0 + kk + s * dlt.  Without sharing every
         // origin has its own kc consecutive matrices (base0 = 0, dlt = kc).  With share_frames,
         // when the chunk's frames lie on that pattern over their sorted distinct list (origins
         // evenly spaced in one trajectory, as the reference places them), each distinct frame
         // is built and diagonalised once and counts in the distributions as often as it is used.
-        int nmat = nbc, base0 = 0, dlt = kc;
+        nmat = nbc;
+        base0 = 0;
+        dlt = kc;
         int *ufr = nullptr;
         if (p.share_frames && T == 1 && St > 1) {
             std::vector<int> uf;
@@ -940,8 +995,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
                 std::vector<int> wgt(nmat, 0);
                 for (int s2 = 0; s2 < St; s2++)
                     for (int kk = 0; kk < kc; kk++) wgt[b0 + kk + s2 * d]++;
-                CK(c->buf[B_UFR].ensure((size_t)nmat * 8));
-                ufr = c->buf[B_UFR].as<int>();
+                CK(buf[B_UFR].ensure((size_t)nmat * 8));
+                ufr = buf[B_UFR].as<int>();
                 CK(cudaMemcpyAsync(ufr, uf.data(), (size_t)nmat * 4, cudaMemcpyHostToDevice, c->stream));
                 CK(cudaMemcpyAsync(ufr + nmat, wgt.data(), (size_t)nmat * 4, cudaMemcpyHostToDevice, c->stream));
             }
@@ -949,16 +1004,16 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         CK(cudaEventRecord(ev[1], c->stream));
         if (ufr)
             k_gather_frames<<<dim3(8, nmat), 256, 0, c->stream>>>(dxyz, dbox, ufr, g.natoms, 1, nmat, nmat, 0,
-                                                                  c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
+                                                                  buf[B_CXYZ].as<float>(), buf[B_CBOX].as<float>());
         else
-            k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(dxyz, dbox, c->buf[B_FIDX].as<int>(), g.natoms, St, kc,
-                                                                 K, k0, c->buf[B_CXYZ].as<float>(), c->buf[B_CBOX].as<float>());
+            k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(dxyz, dbox, buf[B_FIDX].as<int>(), g.natoms, St, kc,
+                                                                 K, k0, buf[B_CXYZ].as<float>(), buf[B_CBOX].as<float>());
         CK(cudaGetLastError());
         launches++;
         BuildArgs a = build_args(c, g);
-        a.xyz = c->buf[B_CXYZ].as<float>();
-        a.box = c->buf[B_CBOX].as<float>();
-        a.ct = c->buf[B_CT].as<float>();
+        a.xyz = buf[B_CXYZ].as<float>();
+        a.box = buf[B_CBOX].as<float>();
+        a.ct = buf[B_CT].as<float>();
         a.H = A;
         a.ldh = ld;
         a.dip = M;                    // frame b: M + b*9*ld, rows 0..2 dipole, 3..8 polarisability
@@ -972,19 +1027,19 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         memset(&e, 0, sizeof e);
         e.A = A;
         e.W = W;
-        e.Z = c->buf[B_Z].as<float>();
-        e.DC = c->buf[B_DC].as<float>();
-        e.DE = c->buf[B_DE].as<float>();
+        e.Z = buf[B_Z].as<float>();
+        e.DC = buf[B_DC].as<float>();
+        e.DE = buf[B_DE].as<float>();
         e.mstride = mstride;
         e.wstride = ld;
         e.n = n;
         e.ld = ld;
-        e.status = c->buf[B_STATUS].as<int>();
-        e.sweeps = c->buf[B_SWEEPS].as<unsigned long long>();
-        e.hist_count = c->buf[B_HCNT].as<unsigned long long>();
-        e.hist_ipr = c->buf[B_HIPR].as<double>();
-        e.hist_mipr = c->buf[B_HMIPR].as<double>();
-        e.out_of_range = c->buf[B_OOR].as<unsigned long long>();
+        e.status = buf[B_STATUS].as<int>();
+        e.sweeps = buf[B_SWEEPS].as<unsigned long long>();
+        e.hist_count = buf[B_HCNT].as<unsigned long long>();
+        e.hist_ipr = buf[B_HIPR].as<double>();
+        e.hist_mipr = buf[B_HMIPR].as<double>();
+        e.out_of_range = buf[B_OOR].as<unsigned long long>();
         e.hist_group = ufr ? 0 : S * kc;   // the chunk's matrices of one trajectory share its histograms
         e.hist_weight = ufr ? ufr + nmat : nullptr;
         e.nomega = nomega;
@@ -1015,14 +1070,14 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
             // spectral density at step 0 of every origin (calcIR.cu:456-482), per trajectory
             for (int s = 0; s < St; s++) {
                 const size_t b = (size_t)base0 + (size_t)s * dlt;
-                CK(cir_launch_spectral(A + b * mstride, ld, W + b * ld, M + b * 9 * ld, ld, n, c->buf[B_MU2].as<float>(),
-                                       c->buf[B_SW].as<double>() + (size_t)(s / S) * nomega, nomega, p.omegaStart,
+                CK(cir_launch_spectral(A + b * mstride, ld, W + b * ld, M + b * 9 * ld, ld, n, buf[B_MU2].as<float>(),
+                                       buf[B_SW].as<double>() + (size_t)(s / S) * nomega, nomega, p.omegaStart,
                                        p.omegaStep, p.t1, p.avef, c->stream, &launches));
             }
             // F = I and the t = 0 vectors (calcIR.cu:577-594)
             if (vectors) {
                 CK(cir_adj_psi_init(M + (size_t)base0 * 9 * ld, (long long)dlt * 9 * ld, ld, n, St,
-                                    c->buf[B_PSI].as<float>(), c->stream));
+                                    buf[B_PSI].as<float>(), c->stream));
             } else {
                 if (split) CK(cir_launch_identity_t(Ft, n, ldh, fs_el, St, c->stream, &launches));
                 else CK(cir_launch_identity(F, n, 2 * ld, (long long)n * 2 * ld, St, c->stream, &launches));
@@ -1031,115 +1086,242 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
             }
             launches++;
         }
-        // the chunk's steps: F <- V_k exp(i L_k dt/hbar) V_k^T F for every origin
-        // (calcIR.cu:596-617), then the correlation terms (calcIR.cu:628-745)
-        auto run_steps = [&](int &nl) -> int {
-            for (int k = k0; k < k0 + kc; k++) {
-                const int kk = k - k0;
-                const size_t mk = (size_t)base0 + kk;      // matrix of origin 0 at this step
-                if (vectors) {
-                    if (k > 0) {
-                        const int rc2 = psi_propagate(c, St, n, ld, A + mk * mstride, (long long)dlt * mstride, W + mk * ld,
-                                                      (long long)dlt * ld, p.dt, c->buf[B_PSI].as<float>(),
-                                                      c->buf[B_LAM].as<float>(), nl);
-                        if (rc2) return rc2;
-                    }
-                    CK(cir_adj_tcf(c->buf[B_PSI].as<float>(), M + mk * 9 * ld, (long long)dlt * 9 * ld, ld, n, St,
-                                   tcf + (size_t)k * 6, (long long)K * 6, c->stream));
-                    nl++;
-                    continue;
-                }
-                if (k > 0 && split) {
-                    CK(cir_launch_split_v(A + mk * mstride, ld, (long long)dlt * mstride, n, Vc, Vr, ldh, vs_el,
-                                          St, c->stream, &nl));
-                    SplitGemmArgs s1{};
-                    s1.Ahi = Vc.hi; s1.Alo = Vc.lo; s1.lda = ldh; s1.sA = vs_el;       // V^T
-                    s1.Bhi = Ft.hi; s1.Blo = Ft.lo; s1.ldb = ldh; s1.sB = fs_el;       // F
-                    s1.Chi = Gt.hi; s1.Clo = Gt.lo; s1.ldc = ldh; s1.sC = fs_el;       // G, transposed
-                    s1.M = n; s1.N = 2 * n; s1.K = n;
-                    s1.epilogue = 1; s1.w = W + mk * ld; s1.wstride = dlt * ld;
-                    s1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
-                    s1.err = c->buf[B_ERR].as<int>();
-                    s1.test_stall = p.test_stall_gemm;
-                    SplitGemmArgs s2 = s1;
-                    s2.Ahi = Vr.hi; s2.Alo = Vr.lo;                                    // V
-                    s2.Bhi = Gt.hi; s2.Blo = Gt.lo;
-                    s2.Chi = Ft.hi; s2.Clo = Ft.lo;                                    // F', transposed
-                    s2.epilogue = 0;
-                    // the step's correlation terms fused into F' = V G
-                    s2.tcf_m0 = M0; s2.tcf_sm0 = 9LL * ld;
-                    s2.tcf_mt = M + mk * 9 * ld; s2.tcf_smt = (long long)dlt * 9 * ld; s2.tcf_ldv = ld;
-                    s2.tcf_out = tcf + (size_t)k * 6; s2.tcf_sout = (long long)K * 6;
-                    s1.tile_n = stile1;
-                    s2.tile_n = stile2;
-                    CK(cir_launch_split_gemm(s1, St, c->stream, &nl));
-                    CK(cir_launch_split_gemm(s2, St, c->stream, &nl));
-                    continue;
-                } else if (k > 0) {
-                    int rc2 = propagate_dev(c, St, n, A + mk * mstride, ld, (long long)dlt * mstride,
-                                            W + mk * ld, dlt * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);
+        if (account) {   // this group's build and eigensolve time, read now (the events are reused)
+            CK(cudaEventSynchronize(ev[3]));
+            float x;
+            cudaEventElapsedTime(&x, ev[1], ev[2]);
+            c->stats.ms_build += x;
+            cudaEventElapsedTime(&x, ev[2], ev[3]);
+            c->stats.ms_eig += x;
+            cudaEventElapsedTime(&x, ev[2], ev[5]);
+            c->stats.ms_tridiag += x;
+        }
+        return CIR_OK;
+    }
+
+    // the split-BF16 products of step k (k > 0): G = V^T F with the phase, F' = V G with the
+    // step's correlation terms fused
+    void split_step(int k, SplitGemmArgs &s1, SplitGemmArgs &s2) const {
+        const size_t mk = (size_t)base0 + (k - k0);
+        s1 = SplitGemmArgs{};
+        s1.Ahi = Vc.hi; s1.Alo = Vc.lo; s1.lda = ldh; s1.sA = vs_el;       // V^T
+        s1.Bhi = Ft.hi; s1.Blo = Ft.lo; s1.ldb = ldh; s1.sB = fs_el;       // F
+        s1.Chi = Gt.hi; s1.Clo = Gt.lo; s1.ldc = ldh; s1.sC = fs_el;       // G, transposed
+        s1.M = n; s1.N = 2 * n; s1.K = n;
+        s1.epilogue = 1; s1.w = W + mk * ld; s1.wstride = dlt * ld;
+        s1.dt_over_hbar = (float)(p.dt / CIR_HBAR);
+        s1.err = c->buf[B_ERR].as<int>();
+        s1.test_stall = p.test_stall_gemm;
+        s2 = s1;
+        s2.Ahi = Vr.hi; s2.Alo = Vr.lo;                                    // V
+        s2.Bhi = Gt.hi; s2.Blo = Gt.lo;
+        s2.Chi = Ft.hi; s2.Clo = Ft.lo;                                    // F', transposed
+        s2.epilogue = 0;
+        // the step's correlation terms fused into F' = V G
+        s2.tcf_m0 = M0; s2.tcf_sm0 = 9LL * ld;
+        s2.tcf_mt = M + mk * 9 * ld; s2.tcf_smt = (long long)dlt * 9 * ld; s2.tcf_ldv = ld;
+        s2.tcf_out = tcf + (size_t)k * 6; s2.tcf_sout = (long long)K * 6;
+        s1.tile_n = stile1;
+        s2.tile_n = stile2;
+    }
+
+    // the chunk's steps: F <- V_k exp(i L_k dt/hbar) V_k^T F for every origin
+    // (calcIR.cu:596-617), then the correlation terms (calcIR.cu:628-745)
+    int steps_launch(int &nl) {
+        for (int k = k0; k < k0 + kc; k++) {
+            const int rc = step_launch(k, nl);
+            if (rc) return rc;
+        }
+        return CIR_OK;
+    }
+
+    // step k of the chunk, every origin of the group
+    int step_launch(int k, int &nl) {
+        {
+            const int kk = k - k0;
+            const size_t mk = (size_t)base0 + kk;      // matrix of origin 0 at this step
+            if (vectors) {
+                if (k > 0) {
+                    const int rc2 = psi_propagate(c, St, n, ld, A + mk * mstride, (long long)dlt * mstride, W + mk * ld,
+                                                  (long long)dlt * ld, p.dt, buf[B_PSI].as<float>(),
+                                                  buf[B_LAM].as<float>(), nl);
                     if (rc2) return rc2;
                 }
-                TcfArgs t;
-                memset(&t, 0, sizeof t);
-                t.F = F;
-                t.sF = (long long)n * 2 * ld;
-                t.m0 = M0;
-                t.sm0 = 9LL * ld;
-                t.mt = M + mk * 9 * ld;
-                t.smt = (long long)dlt * 9 * ld;
-                t.out = tcf + (size_t)k * 6;
-                t.sout = (long long)K * 6;
-                t.n = n;
-                t.ldf = 2 * ld;
-                t.ldv = ld;
-                if (split) {
-                    t.Ft = Ft;
-                    t.sFt = fs_el;
-                    t.ldft = ldh;
-                }
-                CK(cir_launch_tcf(t, St, c->stream, &nl));
+                CK(cir_adj_tcf(buf[B_PSI].as<float>(), M + mk * 9 * ld, (long long)dlt * 9 * ld, ld, n, St,
+                               tcf + (size_t)k * 6, (long long)K * 6, c->stream));
+                nl++;
+                return CIR_OK;
             }
-            return CIR_OK;
-        };
-        if (p.cuda_graphs) {
-            std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2, vs, fs);
-            key.insert(key.end(), {(long long)vectors, (long long)base0, (long long)dlt, (long long)stile1, (long long)stile2,
-                                   (long long)(uintptr_t)c->buf[B_PSI].p, (long long)(uintptr_t)c->buf[B_LAM].p});
-            GraphEntry *ge = nullptr;
-            for (auto &x : c->graphs)
-                if (x.key == key) ge = &x;
-            if (!ge) {
-                int nl = 0;
-                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                const int rc2 = run_steps(nl);
-                cudaGraph_t gr = nullptr;
-                const cudaError_t ce = cudaStreamEndCapture(c->stream, &gr);
-                if (rc2) {
-                    if (gr) cudaGraphDestroy(gr);
-                    return rc2;
-                }
-                if (ce != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "capturing the step loop: %s", cudaGetErrorString(ce));
-                GraphEntry ne;
-                ne.key = key;
-                ne.launches = nl;
-                const cudaError_t ie = cudaGraphInstantiate(&ne.exec, gr, 0);
-                cudaGraphDestroy(gr);
-                if (ie != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "instantiating the step loop: %s", cudaGetErrorString(ie));
-                if (c->graphs.size() >= 32) {
-                    cudaGraphExecDestroy(c->graphs.front().exec);
-                    c->graphs.erase(c->graphs.begin());
-                }
-                c->graphs.push_back(ne);
-                ge = &c->graphs.back();
+            if (k > 0 && split) {
+                CK(cir_launch_split_v(A + mk * mstride, ld, (long long)dlt * mstride, n, Vc, Vr, ldh, vs_el,
+                                      St, c->stream, &nl));
+                SplitGemmArgs s1, s2;
+                split_step(k, s1, s2);
+                CK(cir_launch_split_gemm(s1, St, c->stream, &nl));
+                CK(cir_launch_split_gemm(s2, St, c->stream, &nl));
+                return CIR_OK;
+            } else if (k > 0) {
+                int rc2 = propagate_dev(c, St, n, A + mk * mstride, ld, (long long)dlt * mstride,
+                                        W + mk * ld, dlt * ld, p.dt, F, 2 * ld, (long long)n * 2 * ld, G, nl);
+                if (rc2) return rc2;
             }
-            CK(cudaGraphLaunch(ge->exec, c->stream));
-            launches += ge->launches;
-        } else {
-            int nl = 0;
-            if ((rc = run_steps(nl))) return rc;
-            launches += nl;
+            TcfArgs t;
+            memset(&t, 0, sizeof t);
+            t.F = F;
+            t.sF = (long long)n * 2 * ld;
+            t.m0 = M0;
+            t.sm0 = 9LL * ld;
+            t.mt = M + mk * 9 * ld;
+            t.smt = (long long)dlt * 9 * ld;
+            t.out = tcf + (size_t)k * 6;
+            t.sout = (long long)K * 6;
+            t.n = n;
+            t.ldf = 2 * ld;
+            t.ldv = ld;
+            if (split) {
+                t.Ft = Ft;
+                t.sFt = fs_el;
+                t.ldft = ldh;
+            }
+            CK(cir_launch_tcf(t, St, c->stream, &nl));
         }
+        return CIR_OK;
+    }
+
+    // the key of the chunk's captured step loop
+    std::vector<long long> graph_key() const {
+        std::vector<long long> key = step_key(g, St, K, k0, kc, p.precision, A, W, M, F, G, M0, tcf, tile1, tile2, vs, fs);
+        key.insert(key.end(), {(long long)vectors, (long long)base0, (long long)dlt, (long long)stile1, (long long)stile2,
+                               (long long)(uintptr_t)buf[B_PSI].p, (long long)(uintptr_t)buf[B_LAM].p});
+        return key;
+    }
+
+    // results of every trajectory, after the last chunk (ms_total: the job's device time)
+    int finish(float ms_total) {
+        int rc;
+        count_launch(c, launches);
+        c->stats.frame_steps += steps;
+
+        // results: correlation sums, histograms, spectral density of every trajectory
+        std::vector<double> htcf((size_t)steps * 6), hipr((size_t)T * nomega), hmipr((size_t)T * nomega), hsw((size_t)T * nomega);
+        std::vector<unsigned long long> hcnt((size_t)T * nomega), oor(T);
+        std::vector<int> hst(nb);
+        unsigned long long sweeps = 0;
+        CK(cudaMemcpyAsync(htcf.data(), tcf, (size_t)steps * 48, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hcnt.data(), buf[B_HCNT].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hipr.data(), buf[B_HIPR].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hmipr.data(), buf[B_HMIPR].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hsw.data(), buf[B_SW].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hst.data(), buf[B_STATUS].p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(oor.data(), buf[B_OOR].p, (size_t)T * 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(&sweeps, buf[B_SWEEPS].p, 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->stats.eig_sweeps += (long long)sweeps;
+        for (int i = 0; i < nb; i++)
+            if (hst[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached");
+        if (p.precision != CIR_PREC_FP32 && (rc = check_kernel_flag(c))) return rc;
+
+        for (int tr = 0; tr < T; tr++) {
+            cir_result *r = res + tr;
+            const double *sw_t = hsw.data() + (size_t)tr * nomega, *ipr_t = hipr.data() + (size_t)tr * nomega,
+                         *mipr_t = hmipr.data() + (size_t)tr * nomega;
+            const unsigned long long *cnt_t = hcnt.data() + (size_t)tr * nomega;
+            // sum over origins, T1 damping and 1/nsamples (calcIR.cu:777-782, 798-802, 815-819)
+            std::vector<double> damped[3];
+            for (int q = 0; q < 3; q++) damped[q].assign((size_t)2 * K, 0.0);
+            for (int k = 0; k < K; k++) {
+                CompSum sum[6];
+                for (int s = tr * S; s < (tr + 1) * S; s++)
+                    for (int q = 0; q < 6; q++) sum[q].add(htcf[((size_t)s * K + k) * 6 + q]);
+                const double dcy = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
+                for (int q = 0; q < 3; q++) {
+                    damped[q][2 * k] = sum[2 * q].value() * dcy;
+                    damped[q][2 * k + 1] = sum[2 * q + 1].value() * dcy;
+                }
+            }
+            double *outs[3] = {r->tcf_ir, r->tcf_vv, r->tcf_vh};
+            for (int q = 0; q < 3; q++)
+                if (outs[q]) memcpy(outs[q], damped[q].data(), (size_t)2 * K * 8);
+            // spectral density and frequency distributions (calcIR.cu:831-839)
+            const float norm = (float)(n * S * K);
+            for (int i = 0; i < nomega; i++) {
+                if (r->omega) r->omega[i] = (float)(p.omegaStart + p.omegaStep * i);
+                if (r->sw) r->sw[i] = (float)(sw_t[i] / S);
+                const float pw = (float)((double)cnt_t[i] / p.omegaStep) / norm;
+                if (r->pw) r->pw[i] = pw;
+                if (r->rw) r->rw[i] = ((float)(ipr_t[i] / p.omegaStep) / norm) / pw;
+                if (r->rmw) r->rmw[i] = ((float)(mipr_t[i] / p.omegaStep) / norm) / pw;
+            }
+            // lineshapes (calcIR.cu:786-827, 890-919)
+            float *lsv[3] = {r->ls_ir, r->ls_vv, r->ls_vh};
+            int nls = 0;
+            for (int q = 0; q < 3; q++) {
+                std::vector<double> y;
+                int rc3 = c2r_dev(c, damped[q].data(), y);
+                if (rc3) return rc3;
+                nls = lineshape_rows(&p, y.data(), q == 0 ? r->ls_omega : nullptr, lsv[q]);
+            }
+            r->nls = nls;
+            r->bins_out_of_range = (long long)oor[tr];
+            r->frame_steps_per_s = ms_total > 0 ? steps / (ms_total * 1e-3) : 0.0;
+        }
+        return CIR_OK;
+    }
+};
+
+// The step loop of a chunk: replayed from a captured CUDA graph (cached by key) when the
+// context uses graphs, else launched directly.
+static int step_loop(cir_ctx *c, const std::vector<long long> &key, const std::function<int(int &)> &launch,
+                     int &launches) {
+    if (!c->p.cuda_graphs) {
+        int nl = 0;
+        const int rc = launch(nl);
+        launches += nl;
+        return rc;
+    }
+    GraphEntry *ge = nullptr;
+    for (auto &x : c->graphs)
+        if (x.key == key) ge = &x;
+    if (!ge) {
+        int nl = 0;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc2 = launch(nl);
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(c->stream, &gr);
+        if (rc2) {
+            if (gr) cudaGraphDestroy(gr);
+            return rc2;
+        }
+        if (ce != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "capturing the step loop: %s", cudaGetErrorString(ce));
+        GraphEntry ne;
+        ne.key = key;
+        ne.launches = nl;
+        const cudaError_t ie = cudaGraphInstantiate(&ne.exec, gr, 0);
+        cudaGraphDestroy(gr);
+        if (ie != cudaSuccess) return cir_fail(CIR_ERR_CUDA, "instantiating the step loop: %s", cudaGetErrorString(ie));
+        if (c->graphs.size() >= 32) {
+            cudaGraphExecDestroy(c->graphs.front().exec);
+            c->graphs.erase(c->graphs.begin());
+        }
+        c->graphs.push_back(ne);
+        ge = &c->graphs.back();
+    }
+    CK(cudaGraphLaunch(ge->exec, c->stream));
+    launches += ge->launches;
+    return CIR_OK;
+}
+
+// The frame-steps of one group (see GroupJob), with the context's buffers.
+static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float *dbox, const std::vector<int> &fidx,
+                     cir_result *res, double *ms_run) {
+    GroupJob j(c, c->buf, g, dxyz, dbox, fidx, res);
+    int rc;
+    if ((rc = j.setup(0))) return rc;
+    cudaEvent_t *ev = c->ev;
+    CK(cudaEventRecord(ev[0], c->stream));
+    for (int k0 = 0; k0 < j.K; k0 += j.kn) {
+        if ((rc = j.prepare(k0, std::min(j.kn, j.K - k0), false))) return rc;
+        if ((rc = step_loop(c, j.graph_key(), [&](int &nl) { return j.steps_launch(nl); }, j.launches))) return rc;
         CK(cudaEventRecord(ev[4], c->stream));
         CK(cudaEventSynchronize(ev[4]));
         float x;
@@ -1156,73 +1338,95 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
     CK(cudaEventSynchronize(ev[7]));
     float ms_total = 0;
     cudaEventElapsedTime(&ms_total, ev[0], ev[7]);
-    count_launch(c, launches);
-    c->stats.frame_steps += steps;
     if (ms_run) *ms_run = ms_total;
+    return j.finish(ms_total);
+}
 
-    // results: correlation sums, histograms, spectral density of every trajectory
-    std::vector<double> htcf((size_t)steps * 6), hipr((size_t)T * nomega), hmipr((size_t)T * nomega), hsw((size_t)T * nomega);
-    std::vector<unsigned long long> hcnt((size_t)T * nomega), oor(T);
-    std::vector<int> hst(nb);
-    unsigned long long sweeps = 0;
-    CK(cudaMemcpyAsync(htcf.data(), tcf, (size_t)steps * 48, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hcnt.data(), c->buf[B_HCNT].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hipr.data(), c->buf[B_HIPR].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hmipr.data(), c->buf[B_HMIPR].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hsw.data(), c->buf[B_SW].p, (size_t)T * nomega * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hst.data(), c->buf[B_STATUS].p, (size_t)nb * 4, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(oor.data(), c->buf[B_OOR].p, (size_t)T * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&sweeps, c->buf[B_SWEEPS].p, 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    c->stats.eig_sweeps += (long long)sweeps;
-    for (int i = 0; i < nb; i++)
-        if (hst[i]) return cir_fail(CIR_ERR_NOCONVERGE, "eigensolver sweep cap reached");
-    if (p.precision != CIR_PREC_FP32 && (rc = check_kernel_flag(c))) return rc;
+// Whether cir_run_multi runs the step loops of its size groups jointly (CIR_JOINT=0: one
+// group after another, for comparison).
+static bool joint_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_JOINT");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 
-    for (int tr = 0; tr < T; tr++) {
-        cir_result *r = res + tr;
-        const double *sw_t = hsw.data() + (size_t)tr * nomega, *ipr_t = hipr.data() + (size_t)tr * nomega,
-                     *mipr_t = hmipr.data() + (size_t)tr * nomega;
-        const unsigned long long *cnt_t = hcnt.data() + (size_t)tr * nomega;
-        // sum over origins, T1 damping and 1/nsamples (calcIR.cu:777-782, 798-802, 815-819)
-        std::vector<double> damped[3];
-        for (int q = 0; q < 3; q++) damped[q].assign((size_t)2 * K, 0.0);
-        for (int k = 0; k < K; k++) {
-            CompSum sum[6];
-            for (int s = tr * S; s < (tr + 1) * S; s++)
-                for (int q = 0; q < 6; q++) sum[q].add(htcf[((size_t)s * K + k) * 6 + q]);
-            const double dcy = exp(-1.0 * k * p.dt / (2.0 * p.t1)) / (1. * S);
-            for (int q = 0; q < 3; q++) {
-                damped[q][2 * k] = sum[2 * q].value() * dcy;
-                damped[q][2 * k + 1] = sum[2 * q + 1].value() * dcy;
-            }
-        }
-        double *outs[3] = {r->tcf_ir, r->tcf_vv, r->tcf_vh};
-        for (int q = 0; q < 3; q++)
-            if (outs[q]) memcpy(outs[q], damped[q].data(), (size_t)2 * K * 8);
-        // spectral density and frequency distributions (calcIR.cu:831-839)
-        const float norm = (float)(n * S * K);
-        for (int i = 0; i < nomega; i++) {
-            if (r->omega) r->omega[i] = (float)(p.omegaStart + p.omegaStep * i);
-            if (r->sw) r->sw[i] = (float)(sw_t[i] / S);
-            const float pw = (float)((double)cnt_t[i] / p.omegaStep) / norm;
-            if (r->pw) r->pw[i] = pw;
-            if (r->rw) r->rw[i] = ((float)(ipr_t[i] / p.omegaStep) / norm) / pw;
-            if (r->rmw) r->rmw[i] = ((float)(mipr_t[i] / p.omegaStep) / norm) / pw;
-        }
-        // lineshapes (calcIR.cu:786-827, 890-919)
-        float *lsv[3] = {r->ls_ir, r->ls_vv, r->ls_vh};
-        int nls = 0;
-        for (int q = 0; q < 3; q++) {
-            std::vector<double> y;
-            int rc3 = c2r_dev(c, damped[q].data(), y);
-            if (rc3) return rc3;
-            nls = lineshape_rows(&p, y.data(), q == 0 ? r->ls_omega : nullptr, lsv[q]);
-        }
-        r->nls = nls;
-        r->bins_out_of_range = (long long)oor[tr];
-        r->frame_steps_per_s = ms_total > 0 ? steps / (ms_total * 1e-3) : 0.0;
+// Up to CIR_SPLIT_MAXP size groups of one cir_run_multi job in the split-BF16 form, run in
+// lockstep: per chunk every group's frames are built and diagonalised with its own buffers,
+// then each step of the chunk is one persistent launch of G = V^T F over the origins of all
+// groups and one of F' = V G (each group's correlation terms fused into its tiles), after a
+// small launch per group that splits the step's V into BF16 pairs.  Boxes of different size
+// thus share every propagation launch.  The chunk length is common, and the groups' chunks
+// share the memory budget.
+static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &jobs) {
+    const cir_params &p = c->p;
+    const int K = p.ntcfpoints, ng = (int)jobs.size();
+    size_t budget = (size_t)64 << 30, per = 0;
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
+    int st_max = 1, st_sum = 0;
+    for (auto &j : jobs) {
+        const int St = p.nsamples * j->g.ntraj;
+        per += GroupJob::per_step_bytes(p, j->g) * St;
+        st_max = std::max(st_max, St);
+        st_sum += St;
     }
+    int kn = (int)std::max<size_t>(1, budget / per);
+    if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / st_sum);
+    kn = std::max(1, std::min({kn, K, 65535 / st_max}));
+    int rc;
+    for (auto &j : jobs)
+        if ((rc = j->setup(kn))) return rc;
+    cudaEvent_t *ev = c->ev;
+    int launches = 0;
+    CK(cudaEventRecord(ev[0], c->stream));
+    for (int k0 = 0; k0 < K; k0 += kn) {
+        const int kc = std::min(kn, K - k0);
+        for (auto &j : jobs)
+            if ((rc = j->prepare(k0, kc, true))) return rc;
+        CK(cudaEventRecord(ev[3], c->stream));
+        std::vector<long long> key = {-1, ng};
+        for (auto &j : jobs) {
+            const std::vector<long long> kj = j->graph_key();
+            key.insert(key.end(), kj.begin(), kj.end());
+        }
+        auto launch = [&](int &nl) -> int {
+            for (int k = k0; k < k0 + kc; k++) {
+                if (k == 0) {   // the step-0 correlation terms of every group (F = I)
+                    for (auto &j : jobs)
+                        if (int r = j->step_launch(0, nl)) return r;
+                    continue;
+                }
+                SplitGemmArgs s1[CIR_SPLIT_MAXP], s2[CIR_SPLIT_MAXP];
+                int batch[CIR_SPLIT_MAXP];
+                for (int i = 0; i < ng; i++) {
+                    GroupJob &j = *jobs[i];
+                    const size_t mk = (size_t)j.base0 + (k - j.k0);
+                    CK(cir_launch_split_v(j.A + mk * j.mstride, j.ld, (long long)j.dlt * j.mstride, j.n, j.Vc, j.Vr, j.ldh,
+                                          j.vs_el, j.St, c->stream, &nl));
+                    j.split_step(k, s1[i], s2[i]);
+                    batch[i] = j.St;
+                }
+                CK(cir_launch_split_gemm_multi(s1, batch, ng, c->stream, &nl));
+                CK(cir_launch_split_gemm_multi(s2, batch, ng, c->stream, &nl));
+            }
+            return CIR_OK;
+        };
+        if ((rc = step_loop(c, key, launch, launches))) return rc;
+        CK(cudaEventRecord(ev[4], c->stream));
+        CK(cudaEventSynchronize(ev[4]));
+        float x;
+        cudaEventElapsedTime(&x, ev[3], ev[4]);
+        c->stats.ms_prop += x;
+    }
+    CK(cudaEventRecord(ev[7], c->stream));
+    CK(cudaEventSynchronize(ev[7]));
+    float ms_total = 0;
+    cudaEventElapsedTime(&ms_total, ev[0], ev[7]);
+    count_launch(c, launches);
+    for (auto &j : jobs)
+        if ((rc = j->finish(ms_total))) return rc;
     return CIR_OK;
 }
 
@@ -1280,7 +1484,62 @@ extern "C" int cir_run_multi(cir_ctx *c, int ntraj, const cir_traj_in *traj, cir
             return cir_fail(CIR_ERR_NONFINITE, "trajectory %d: box contains NaN or Inf", i);
         groups[t.natoms].push_back(i);
     }
+    // the split-BF16 form runs up to CIR_SPLIT_MAXP size groups jointly (every step one
+    // launch per product for all of them); the other forms and options group by group
+    const bool joint = joint_enabled() && p.precision == CIR_PREC_BF16X3 && !p.share_frames && !p.propagate_vectors &&
+                       groups.size() > 1;
+    std::vector<std::vector<int>> batches;   // the group ids (natoms) of each joint run
+    if (joint) {
+        std::vector<int> keys;
+        for (auto &kv : groups) keys.push_back(kv.first);
+        for (size_t i = 0; i < keys.size(); i += CIR_SPLIT_MAXP)
+            batches.emplace_back(keys.begin() + i, keys.begin() + std::min(keys.size(), i + (size_t)CIR_SPLIT_MAXP));
+    }
+    for (const auto &bt : batches) {
+        while (c->gbuf.size() + 1 < bt.size()) c->gbuf.emplace_back(new DevBuf[B_COUNT]);
+        std::vector<std::unique_ptr<GroupJob>> jobs;
+        std::vector<std::vector<int>> fidxs(bt.size());
+        std::vector<std::vector<cir_result>> rss(bt.size());
+        for (size_t gi = 0; gi < bt.size(); gi++) {
+            const int natoms = bt[gi];
+            const std::vector<int> &ids = groups[natoms];
+            DevBuf *buf = gi == 0 ? c->buf : c->gbuf[gi - 1].get();
+            Group g;
+            g.natoms = natoms;
+            g.nmol = natoms / p.natom_mol;
+            g.n = g.nmol * p.nchrom_mol;
+            g.ld = (g.n + 3) & ~3;
+            g.ntraj = (int)ids.size();
+            long long nf = 0;
+            for (int i : ids) nf += traj[i].nframes;
+            CK(buf[B_XYZ].ensure((size_t)nf * natoms * 12));
+            CK(buf[B_BOX].ensure((size_t)nf * 12));
+            fidxs[gi].resize((size_t)g.ntraj * steps);
+            long long off = 0;
+            for (int j = 0; j < g.ntraj; j++) {
+                const cir_traj_in &t = traj[ids[j]];
+                CK(cudaMemcpyAsync(buf[B_XYZ].as<float>() + (size_t)off * natoms * 3, t.xyz,
+                                   (size_t)t.nframes * natoms * 12, cudaMemcpyDefault, c->stream));
+                CK(cudaMemcpyAsync(buf[B_BOX].as<float>() + (size_t)off * 3, t.box, (size_t)t.nframes * 12,
+                                   cudaMemcpyDefault, c->stream));
+                for (long long k = 0; k < steps; k++)
+                    fidxs[gi][(size_t)j * steps + k] = (int)(off + (t.frame_of_step ? t.frame_of_step[k] : k));
+                off += t.nframes;
+            }
+            rss[gi].resize(g.ntraj);
+            for (int j = 0; j < g.ntraj; j++) rss[gi][j] = results[ids[j]];
+            jobs.emplace_back(new GroupJob(c, buf, g, buf[B_XYZ].as<float>(), buf[B_BOX].as<float>(), fidxs[gi],
+                                           rss[gi].data()));
+        }
+        const int rc = run_groups_joint(c, jobs);
+        if (rc) return rc;
+        for (size_t gi = 0; gi < bt.size(); gi++) {
+            const std::vector<int> &ids = groups[bt[gi]];
+            for (size_t j = 0; j < ids.size(); j++) results[ids[j]] = rss[gi][j];
+        }
+    }
     for (auto &kv : groups) {
+        if (joint) break;
         const int natoms = kv.first;
         const std::vector<int> &ids = kv.second;
         Group g;

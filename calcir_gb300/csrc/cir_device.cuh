@@ -219,6 +219,12 @@ struct SplitGemmArgs {
 };
 size_t cir_split_ld(int n);   // leading dimension of the split operands (n rounded up to 8)
 cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches);
+// Several split-BF16 products in one persistent launch (the tiles of problem 0 first, then
+// problem 1, ...): each problem a batch of one shape with its own operands, epilogue and
+// tensor maps, all in the widest tile width any of them takes; bz0 must be 0.
+constexpr int CIR_SPLIT_MAXP = 4;
+cudaError_t cir_launch_split_gemm_multi(const SplitGemmArgs *g, const int *batch, int np, cudaStream_t s,
+                                        int *launches);
 // Vc = V (V[k][i] at A[i*ld + k]) and Vr = V^T, both as Vc[i*ldh + k]-style K-major pairs
 cudaError_t cir_launch_split_v(const float *A, int ld, long long sA, int n, SplitMat Vc, SplitMat Vr, int ldh,
                                long long sV, int batch, cudaStream_t s, int *launches);

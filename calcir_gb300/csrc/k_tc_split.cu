@@ -332,13 +332,33 @@ __global__ void __launch_bounds__(QT) k_tc_split(const __grid_constant__ SplitMa
 constexpr int PT = 320;                       // threads: producer, MMA, eight epilogue warps
 constexpr int PEW = 8;                        // epilogue warps
 
+// The products one persistent launch walks: up to CIR_SPLIT_MAXP problems (each a batch of
+// one shape, e.g. the origins of one box size), their tiles numbered problem after problem.
+struct PersistPlan {
+    SplitMaps maps[CIR_SPLIT_MAXP];
+    SplitGemmArgs g[CIR_SPLIT_MAXP];
+    int tiles_n[CIR_SPLIT_MAXP], tiles_mn[CIR_SPLIT_MAXP], first[CIR_SPLIT_MAXP + 1];
+    int np;
+};
+
+// problem, batch entry and tile origin of tile t of a plan
+__device__ __forceinline__ int plan_tile(const PersistPlan &plan, int t, int &bz, int &m0, int &n0, int qn) {
+    int pi = 0;
+    while (pi + 1 < plan.np && t >= plan.first[pi + 1]) pi++;
+    const int lt = t - plan.first[pi], rem = lt % plan.tiles_mn[pi];
+    bz = lt / plan.tiles_mn[pi] + plan.g[pi].bz0;
+    m0 = (rem / plan.tiles_n[pi]) * QM;
+    n0 = (rem % plan.tiles_n[pi]) * qn;
+    return pi;
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
 template <int QK, int QS, int QN>
-__global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ SplitMaps maps, SplitGemmArgs g,
-                                                      int tiles_n, int tiles_mn, int ntiles) {
+__global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ PersistPlan plan) {
+    const int ntiles = plan.first[plan.np];
     using C = QCfg<QK, QS, QN>;
     constexpr int TA = C::TILE_A, TB = C::TILE_B, Q_STAGE = C::STAGE;
     constexpr uint32_t Q_IDESC = make_idesc_mn(1u, QM, QN);
@@ -385,13 +405,13 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    const int KT = (g.K + QK - 1) / QK;
     // the pipeline's waits; the fault drill shortens them so that they run out quickly (the
     // waits for copies and MMAs in flight before the CTA exits always keep the full limit)
-    const long long lim = g.test_stall ? (1ll << 14) : WAIT_LIMIT;
+    const bool stall = plan.g[0].test_stall != 0;
+    const long long lim = stall ? (1ll << 14) : WAIT_LIMIT;
     auto fail = [&]() {
         *abort_flag = 1;
-        if (g.err) atomicExch(g.err, 1);
+        if (plan.g[0].err) atomicExch(plan.g[0].err, 1);
     };
 
     if (warp == 0) {
@@ -399,8 +419,10 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             uint32_t it = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok && !*abort_flag; t += gridDim.x) {
-                const int bz = t / tiles_mn + g.bz0, rem = t % tiles_mn;
-                const int m0 = (rem / tiles_n) * QM, n0 = (rem % tiles_n) * QN;
+                int bz, m0, n0;
+                const int pi = plan_tile(plan, t, bz, m0, n0, QN);
+                const SplitMaps &maps = plan.maps[pi];
+                const int KT = (plan.g[pi].K + QK - 1) / QK;
                 for (int kt = 0; kt < KT; kt++, it++) {
                     const int s = it % QS;
                     if (it >= QS && !(ok = mbar_wait(&empty[s], ((it / QS) & 1) ^ 1, lim))) break;
@@ -424,6 +446,8 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             int li = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, li++) {
                 const int a = li & 1;
+                int bz_, m0_, n0_;
+                const int KT = (plan.g[plan_tile(plan, t, bz_, m0_, n0_, QN)].K + QK - 1) / QK;
                 if (li >= 2 && !(ok = mbar_wait(&tempty[a], ((li >> 1) & 1) ^ 1, lim))) break;
                 if (*abort_flag) break;
                 fence_after();
@@ -448,7 +472,7 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
                 if (!ok) break;
                 // fault drill: the first tile's completion is never signalled, so the epilogue's
                 // wait on it (and then every other role's) runs out
-                if (!(g.test_stall && li == 0)) mma_commit(&tfull[a]);
+                if (!(stall && li == 0)) mma_commit(&tfull[a]);
             }
             if (!ok) fail();
             if (issued) {   // every MMA issued has completed before the accumulators are freed
@@ -459,7 +483,6 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
     } else {
         const int quarter = warp & 3, row = quarter * 32 + lane;
         const int cbeg = ((warp - 2) >> 2) * (QN / 2), cend = cbeg + QN / 2;   // this warp's columns
-        const bool fuse = g.tcf_out != nullptr;
         int li = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
             const int a = li & 1;
@@ -469,8 +492,9 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Sp
             }
             if (*abort_flag) break;
             fence_after();
-            const int bz = t / tiles_mn + g.bz0, rem = t % tiles_mn;
-            const int m0 = (rem / tiles_n) * QM, n0 = (rem % tiles_n) * QN;
+            int bz, m0, n0;
+            const SplitGemmArgs &g = plan.g[plan_tile(plan, t, bz, m0, n0, QN)];
+            const bool fuse = g.tcf_out != nullptr;
             const int r = m0 + row;
             float pr[9], pi[9];
             #pragma unroll
@@ -773,48 +797,91 @@ static bool make_map(CUtensorMap *m, const __nv_bfloat16 *base, int K, int rows,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches) {
-    if (batch < 1 || batch > 65535 || g.M < 1 || g.N < 1 || g.K < 1 || (g.epilogue == 1 && (g.N & 1)))
-        return cudaErrorInvalidValue;
-    if ((g.lda & 7) || (g.ldb & 7) || (g.sA & 7) || (g.sB & 7) || g.lda < g.K || g.ldb < g.K) return cudaErrorInvalidValue;
-    if ((long long)g.lda * g.M > g.sA && batch > 1) return cudaErrorInvalidValue;
-    if ((long long)g.ldb * g.N > g.sB && batch > 1) return cudaErrorInvalidValue;
+// checks of one split-BF16 problem
+static bool split_ok(const SplitGemmArgs &g, int batch) {
+    if (batch < 1 || batch > 65535 || g.M < 1 || g.N < 1 || g.K < 1 || (g.epilogue == 1 && (g.N & 1))) return false;
+    if ((g.lda & 7) || (g.ldb & 7) || (g.sA & 7) || (g.sB & 7) || g.lda < g.K || g.ldb < g.K) return false;
+    if ((long long)g.lda * g.M > g.sA && batch > 1) return false;
+    if ((long long)g.ldb * g.N > g.sB && batch > 1) return false;
     for (const void *p : {(const void *)g.Ahi, (const void *)g.Alo, (const void *)g.Bhi, (const void *)g.Blo})
-        if (reinterpret_cast<uintptr_t>(p) & 15) return cudaErrorInvalidValue;
-    constexpr int QK = 32;   // 64-byte swizzle; 3 x 32 KB stages (two CTAs per SM), or for
-                             // products of at most 4 K slices 2 stages (three CTAs per SM)
-    SplitMaps maps;
-    const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
+        if (reinterpret_cast<uintptr_t>(p) & 15) return false;
+    return true;
+}
+
+// the tile width a problem takes by itself
+static int split_width(const SplitGemmArgs &g) {
+    constexpr int QK = 32;
+    if (g.tile_n == 128 || g.tile_n == 256) return g.tile_n;
     // 128 x 256 tiles for the wide products (the propagation) and the back-transform updates
     // (C = D - A B): a quarter less operand traffic per flop
-    const int qn = (g.tile_n == 128 || g.tile_n == 256)
-                       ? g.tile_n
-                       : (((g.N >= 1024 && g.K > 4 * QK) || (g.epilogue == 2 && g.N >= 256)) ? 256 : 128);
-    if (!make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK, QM) ||
-        !make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch, QK, QM) ||
-        !make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) ||
-        !make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, qn))
-        return cudaErrorInvalidValue;
+    return ((g.N >= 1024 && g.K > 4 * QK) || (g.epilogue == 2 && g.N >= 256)) ? 256 : 128;
+}
+
+static bool split_maps(const SplitGemmArgs &g, int batch, int qn, SplitMaps &maps) {
+    constexpr int QK = 32;
+    const long long sA = batch > 1 ? g.sA : (long long)g.lda * g.M, sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
+    return make_map(&maps.a_hi, g.Ahi, g.K, g.M, g.lda, sA, batch, QK, QM) &&
+           make_map(&maps.a_lo, g.Alo, g.K, g.M, g.lda, sA, batch, QK, QM) &&
+           make_map(&maps.b_hi, g.Bhi, g.K, g.N, g.ldb, sB, batch, QK, qn) &&
+           make_map(&maps.b_lo, g.Blo, g.K, g.N, g.ldb, sB, batch, QK, qn);
+}
+
+// One persistent launch over np problems (the tiles of problem 0 first), all in tiles of width qn.
+static cudaError_t launch_persist(const SplitGemmArgs *g, const int *batch, int np, int qn, cudaStream_t s,
+                                  int *launches) {
+    constexpr int QK = 32;
+    PersistPlan plan;
+    memset(&plan, 0, sizeof plan);
+    plan.np = np;
+    long long ntl = 0;
+    for (int i = 0; i < np; i++) {
+        if (!split_maps(g[i], batch[i], qn, plan.maps[i])) return cudaErrorInvalidValue;
+        plan.g[i] = g[i];
+        plan.tiles_n[i] = (g[i].N + qn - 1) / qn;
+        plan.tiles_mn[i] = plan.tiles_n[i] * ((g[i].M + QM - 1) / QM);
+        plan.first[i] = (int)ntl;
+        ntl += (long long)plan.tiles_mn[i] * batch[i];
+        if (ntl > INT32_MAX) return cudaErrorInvalidValue;
+    }
+    plan.first[np] = (int)ntl;
+    const int grid = (int)std::min<long long>(ntl, sm_count());
+    auto go = [&](auto kern, size_t smem) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, PT, smem, s>>>(plan);
+        return cudaGetLastError();
+    };
+    const cudaError_t e = qn == 256 ? go(k_tc_persist<QK, 4, 256>, QCfg<QK, 4, 256>::SMEM)
+                                    : go(k_tc_persist<QK, 6, 128>, QCfg<QK, 6, 128>::SMEM);
+    if (e == cudaSuccess && launches) *launches += 1;
+    return e;
+}
+
+cudaError_t cir_launch_split_gemm_multi(const SplitGemmArgs *g, const int *batch, int np, cudaStream_t s,
+                                        int *launches) {
+    if (np < 1 || np > CIR_SPLIT_MAXP) return cudaErrorInvalidValue;
+    int qn = 0;
+    for (int i = 0; i < np; i++) {
+        if (!split_ok(g[i], batch[i]) || g[i].bz0 != 0) return cudaErrorInvalidValue;
+        qn = std::max(qn, split_width(g[i]));
+    }
+    return launch_persist(g, batch, np, qn, s, launches);
+}
+
+cudaError_t cir_launch_split_gemm(const SplitGemmArgs &g, int batch, cudaStream_t s, int *launches) {
+    if (!split_ok(g, batch)) return cudaErrorInvalidValue;
+    constexpr int QK = 32;   // 64-byte swizzle; 3 x 32 KB stages (two CTAs per SM), or for
+                             // products of at most 4 K slices 2 stages (three CTAs per SM)
+    const int qn = split_width(g);
+    SplitMaps maps;
+    if (!split_maps(g, batch, qn, maps)) return cudaErrorInvalidValue;
+    const long long sB = batch > 1 ? g.sB : (long long)g.ldb * g.N;
     // persistent warp-specialised CTAs (one per SM), the epilogue of one tile overlapping the
     // loads and MMAs of the next: 128 x 256 tiles in a 4-stage ring for the propagation,
     // 128 x 128 tiles in a 6-stage ring otherwise
     if (g.bz0 == 0 && persist_enabled()) {
-        const int tiles_n = (g.N + qn - 1) / qn, tiles_mn = tiles_n * ((g.M + QM - 1) / QM);
-        const long long ntl = (long long)tiles_mn * batch;
-        if (ntl <= INT32_MAX) {
-            const int grid = (int)std::min<long long>(ntl, sm_count());
-            auto go = [&](auto kern, size_t smem) -> cudaError_t {
-                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (e != cudaSuccess) return e;
-                kern<<<grid, PT, smem, s>>>(maps, g, tiles_n, tiles_mn, (int)ntl);
-                return cudaGetLastError();
-            };
-            const cudaError_t e = qn == 256 ? go(k_tc_persist<QK, 4, 256>, QCfg<QK, 4, 256>::SMEM)
-                                            : go(k_tc_persist<QK, 6, 128>, QCfg<QK, 6, 128>::SMEM);
-            if (e != cudaSuccess) return e;
-            if (launches) *launches += 1;
-            return cudaSuccess;
-        }
+        const long long ntl = (long long)((g.N + qn - 1) / qn) * ((g.M + QM - 1) / QM) * batch;
+        if (ntl <= INT32_MAX) return launch_persist(&g, &batch, 1, qn, s, launches);
     }
     if (qn == 256) {
         // Wave quantisation: two 128 x 256 CTAs per SM.  When the last wave of the batch would

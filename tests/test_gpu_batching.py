@@ -161,3 +161,24 @@ def test_autotuner_tensor_core_forms_agree(lib):
     assert st["tuned_tridiag_blocks"] in (3, 4), st      # order 128: four blocks per SM by default
     print("autotuner picked", st["tuned_split_tile"], "wide tiles,", st["tuned_tridiag_blocks"], "blocks per SM")
     _same(on, off, 1e-6, "autotuned tensor-core form")
+
+
+def test_run_multi_joint_split_launches_match_single_runs(lib):
+    """The split-BF16 form runs the step loops of up to four box sizes jointly: each step is
+    one persistent launch per product over the origins of every size.  Each trajectory's
+    results equal what cir_run gives for it alone in the same form (the same products, tile
+    by tile), and the joint job launches fewer kernels than the sizes one after another."""
+    prm, p = _params(lib, precision="bf16x3")
+    sizes = [16, 27, 16, 40, 27]
+    trajs = _trajectories(lib, prm, sizes)
+    with lib.Engine(p, sizes[0] * 4) as eng:
+        multi = eng.run_multi(trajs)
+        joint_launches = eng.stats()["kernel_launches"]
+    single_launches = 0
+    for i, (xyz, box, fos) in enumerate(trajs):
+        with lib.Engine(p, xyz.shape[1]) as eng:
+            single = eng.run(xyz, box, fos)
+            single_launches += eng.stats()["kernel_launches"]
+        _same(multi[i], single, 1e-5, f"trajectory {i} ({sizes[i]} molecules), joint split-BF16")
+    print("kernel launches: joint", joint_launches, "one size at a time", single_launches)
+    assert joint_launches < single_launches
