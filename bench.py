@@ -131,11 +131,12 @@ def gpu_identifier():
 
 # DRAM bytes (read + write) per 1024 x 1024 matrix of the tridiagonalisation kernel, from one
 # ncu capture of k_eigh_tq on 152 matrices of order 1024 (dram__bytes_read.sum +
-# dram__bytes_write.sum over the launch, / 152):
+# dram__bytes_write.sum over the launch, / 152: 86.17 GB + 3.48 GB read and written, with
+# the tiles of the matrix-vector products walked in alternating order):
 #   python -m calcir_gb300.profile eigh --nmol 512 --batch 152 && \
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_eigh_tq -c 1 \
 #       python -m calcir_gb300.profile eigh --nmol 512 --batch 152
-TRIDIAG_DRAM_BYTES_PER_MATRIX = 0.666e9
+TRIDIAG_DRAM_BYTES_PER_MATRIX = 0.590e9
 
 
 def tridiag_bytes(n, nb=32):

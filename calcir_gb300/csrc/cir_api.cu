@@ -1357,42 +1357,55 @@ static bool joint_enabled() {
 // then each step of the chunk is one persistent launch of G = V^T F over the origins of all
 // groups and one of F' = V G (each group's correlation terms fused into its tiles), after a
 // small launch per group that splits the step's V into BF16 pairs.  Boxes of different size
-// thus share every propagation launch.  The chunk length is common, and the groups' chunks
-// share the memory budget.
+// thus share every propagation launch.  Each group has its own chunk length; the steps run
+// jointly up to the first end of a prepared chunk, where that group prepares its next one.
 static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &jobs) {
     const cir_params &p = c->p;
     const int K = p.ntcfpoints, ng = (int)jobs.size();
-    size_t budget = (size_t)64 << 30, per = 0;
+    // chunk lengths: the groups' chunks are resident together, so they share the memory
+    // budget; the smaller groups take whole chunks first (their eigensolver launches stay
+    // large), the largest group the rest
+    size_t budget = (size_t)64 << 30;
     size_t freeb = 0, totalb = 0;
-    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
-    int st_max = 1, st_sum = 0;
-    for (auto &j : jobs) {
-        const int St = p.nsamples * j->g.ntraj;
-        per += GroupJob::per_step_bytes(p, j->g) * St;
-        st_max = std::max(st_max, St);
-        st_sum += St;
+    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget * ng, freeb / 2);
+    std::vector<size_t> per(ng);
+    std::vector<int> order(ng), kn(ng);
+    for (int i = 0; i < ng; i++) {
+        per[i] = GroupJob::per_step_bytes(p, jobs[i]->g) * (size_t)(p.nsamples * jobs[i]->g.ntraj);
+        order[i] = i;
     }
-    int kn = (int)std::max<size_t>(1, budget / per);
-    if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / st_sum);
-    kn = std::max(1, std::min({kn, K, 65535 / st_max}));
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return per[x] < per[y]; });
+    size_t left = budget;
+    for (int r = 0; r < ng; r++) {
+        const int i = order[r];
+        const size_t share = left / (ng - r);
+        kn[i] = (int)std::max<size_t>(1, std::min<size_t>(K, share / per[i]));
+        if (p.batch_frames > 0) kn[i] = std::max(1, std::min(K, p.batch_frames / (p.nsamples * jobs[i]->g.ntraj)));
+        left -= std::min(left, (size_t)kn[i] * per[i]);
+    }
     int rc;
-    for (auto &j : jobs)
-        if ((rc = j->setup(kn))) return rc;
+    for (int i = 0; i < ng; i++)
+        if ((rc = jobs[i]->setup(kn[i]))) return rc;   // setup may shorten kn (grid limits)
     cudaEvent_t *ev = c->ev;
     int launches = 0;
+    std::vector<int> next(ng, 0);   // first step not covered by each group's prepared chunk
     CK(cudaEventRecord(ev[0], c->stream));
-    for (int k0 = 0; k0 < K; k0 += kn) {
-        const int kc = std::min(kn, K - k0);
-        for (auto &j : jobs)
-            if ((rc = j->prepare(k0, kc, true))) return rc;
+    for (int k0 = 0; k0 < K;) {
+        for (int i = 0; i < ng; i++)
+            if (next[i] == k0) {
+                GroupJob &j = *jobs[i];
+                if ((rc = j.prepare(k0, std::min(j.kn, K - k0), true))) return rc;
+                next[i] = k0 + j.kc;
+            }
+        const int k1 = *std::min_element(next.begin(), next.end());   // steps k0 .. k1 - 1 run jointly
         CK(cudaEventRecord(ev[3], c->stream));
-        std::vector<long long> key = {-1, ng};
+        std::vector<long long> key = {-1, ng, k0, k1};
         for (auto &j : jobs) {
             const std::vector<long long> kj = j->graph_key();
             key.insert(key.end(), kj.begin(), kj.end());
         }
         auto launch = [&](int &nl) -> int {
-            for (int k = k0; k < k0 + kc; k++) {
+            for (int k = k0; k < k1; k++) {
                 if (k == 0) {   // the step-0 correlation terms of every group (F = I)
                     for (auto &j : jobs)
                         if (int r = j->step_launch(0, nl)) return r;
@@ -1419,6 +1432,7 @@ static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &
         float x;
         cudaEventElapsedTime(&x, ev[3], ev[4]);
         c->stats.ms_prop += x;
+        k0 = k1;
     }
     CK(cudaEventRecord(ev[7], c->stream));
     CK(cudaEventSynchronize(ev[7]));

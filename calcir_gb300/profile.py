@@ -43,6 +43,7 @@ def prop(n: int, nprop: int, precision: str = "fp32") -> None:
 
 
 def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32", **options) -> None:
+    """One job; autotune=0 keeps the autotuner's trial launches out of a capture."""
     p = cg.default_params(model="tip4p2005", species="H2O", ntcfpoints=ntcf, nsamples=nsamples, sampleEvery=2.0,
                           avef=3415.0, omegaStart=1000, omegaStop=5000, omegaStep=1, precision=precision, **options)
     fos = cg.frame_table(p, 0.010)
@@ -79,6 +80,7 @@ def main() -> None:
     r.add_argument("--nsamples", type=int, default=10)
     r.add_argument("--ntcf", type=int, default=250)
     r.add_argument("--precision", default="fp32")
+    r.add_argument("--autotune", type=int, default=1)
     for opt in ("propagate-vectors", "share-frames", "refine-eigen"):
         r.add_argument("--" + opt, type=int, default=0)
     gr = sub.add_parser("grad")
@@ -94,7 +96,7 @@ def main() -> None:
         grad(a.nmol, a.nsamples, a.ntcf)
     else:
         run(a.nmol, a.nsamples, a.ntcf, a.precision, propagate_vectors=a.propagate_vectors,
-            share_frames=a.share_frames, refine_eigen=a.refine_eigen)
+            share_frames=a.share_frames, refine_eigen=a.refine_eigen, autotune=a.autotune)
 
 
 if __name__ == "__main__":
