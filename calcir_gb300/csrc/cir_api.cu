@@ -1357,32 +1357,28 @@ static bool joint_enabled() {
 // then each step of the chunk is one persistent launch of G = V^T F over the origins of all
 // groups and one of F' = V G (each group's correlation terms fused into its tiles), after a
 // small launch per group that splits the step's V into BF16 pairs.  Boxes of different size
-// thus share every propagation launch.  Each group has its own chunk length; the steps run
-// jointly up to the first end of a prepared chunk, where that group prepares its next one.
+// thus share every propagation launch.  The steps run jointly up to the first end of a
+// prepared chunk, where that group prepares its next one (the chunks are of equal length
+// unless a group's grid limit shortens its own).
 static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &jobs) {
     const cir_params &p = c->p;
     const int K = p.ntcfpoints, ng = (int)jobs.size();
-    // chunk lengths: the groups' chunks are resident together, so they share the memory
-    // budget; the smaller groups take whole chunks first (their eigensolver launches stay
-    // large), the largest group the rest
+    // chunk length: the groups' chunks are resident together, so they share the memory budget;
+    // one length for all, balanced over the job (equal chunks keep every eigensolver launch
+    // many waves long)
     size_t budget = (size_t)64 << 30;
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget * ng, freeb / 2);
-    std::vector<size_t> per(ng);
-    std::vector<int> order(ng), kn(ng);
-    for (int i = 0; i < ng; i++) {
-        per[i] = GroupJob::per_step_bytes(p, jobs[i]->g) * (size_t)(p.nsamples * jobs[i]->g.ntraj);
-        order[i] = i;
+    size_t per = 0;
+    int st_sum = 0;
+    for (auto &j : jobs) {
+        per += GroupJob::per_step_bytes(p, j->g) * (size_t)(p.nsamples * j->g.ntraj);
+        st_sum += p.nsamples * j->g.ntraj;
     }
-    std::sort(order.begin(), order.end(), [&](int x, int y) { return per[x] < per[y]; });
-    size_t left = budget;
-    for (int r = 0; r < ng; r++) {
-        const int i = order[r];
-        const size_t share = left / (ng - r);
-        kn[i] = (int)std::max<size_t>(1, std::min<size_t>(K, share / per[i]));
-        if (p.batch_frames > 0) kn[i] = std::max(1, std::min(K, p.batch_frames / (p.nsamples * jobs[i]->g.ntraj)));
-        left -= std::min(left, (size_t)kn[i] * per[i]);
-    }
+    int kmax = (int)std::max<size_t>(1, std::min<size_t>(K, budget / per));
+    if (p.batch_frames > 0) kmax = std::max(1, std::min(K, p.batch_frames / st_sum));
+    const int nchunk = (K + kmax - 1) / kmax;
+    std::vector<int> kn(ng, (K + nchunk - 1) / nchunk);
     int rc;
     for (int i = 0; i < ng; i++)
         if ((rc = jobs[i]->setup(kn[i]))) return rc;   // setup may shorten kn (grid limits)
