@@ -1357,28 +1357,38 @@ static bool joint_enabled() {
 // then each step of the chunk is one persistent launch of G = V^T F over the origins of all
 // groups and one of F' = V G (each group's correlation terms fused into its tiles), after a
 // small launch per group that splits the step's V into BF16 pairs.  Boxes of different size
-// thus share every propagation launch.  The steps run jointly up to the first end of a
-// prepared chunk, where that group prepares its next one (the chunks are of equal length
-// unless a group's grid limit shortens its own).
+// thus share every propagation launch.  Each group keeps the chunk length it would take
+// alone; the steps run jointly up to the first end of a prepared chunk, where that group
+// prepares its next one.
 static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &jobs) {
     const cir_params &p = c->p;
     const int K = p.ntcfpoints, ng = (int)jobs.size();
-    // chunk length: the groups' chunks are resident together, so they share the memory budget;
-    // one length for all, balanced over the job (equal chunks keep every eigensolver launch
-    // many waves long)
-    size_t budget = (size_t)64 << 30;
+    // chunk lengths: each group takes the chunks it would take alone (up to 64 GiB, balanced
+    // so that its chunks are of equal length and every eigensolver launch stays many waves
+    // long); the groups' chunks are resident together, so when their sum exceeds 60% of the
+    // free memory every group's share shrinks in proportion
     size_t freeb = 0, totalb = 0;
-    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget * ng, freeb / 2);
-    size_t per = 0;
-    int st_sum = 0;
-    for (auto &j : jobs) {
-        per += GroupJob::per_step_bytes(p, j->g) * (size_t)(p.nsamples * j->g.ntraj);
-        st_sum += p.nsamples * j->g.ntraj;
+    size_t budget = (size_t)64 << 30;
+    if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget * ng, freeb / 10 * 6);
+    std::vector<size_t> per(ng);
+    for (int i = 0; i < ng; i++)
+        per[i] = GroupJob::per_step_bytes(p, jobs[i]->g) * (size_t)(p.nsamples * jobs[i]->g.ntraj);
+    auto balanced = [&](double cap_bytes, int i) {
+        int km = (int)std::max(1.0, std::min((double)K, cap_bytes / (double)per[i]));
+        if (p.batch_frames > 0) km = std::max(1, std::min(K, p.batch_frames / (p.nsamples * jobs[i]->g.ntraj)));
+        const int nc = (K + km - 1) / km;
+        return (K + nc - 1) / nc;
+    };
+    std::vector<int> kn(ng);
+    double cap = (double)((size_t)64 << 30);
+    for (int it = 0; it < 64; it++, cap *= 0.9) {
+        size_t total = 0;
+        for (int i = 0; i < ng; i++) {
+            kn[i] = balanced(cap, i);
+            total += (size_t)kn[i] * per[i];
+        }
+        if (total <= budget) break;
     }
-    int kmax = (int)std::max<size_t>(1, std::min<size_t>(K, budget / per));
-    if (p.batch_frames > 0) kmax = std::max(1, std::min(K, p.batch_frames / st_sum));
-    const int nchunk = (K + kmax - 1) / kmax;
-    std::vector<int> kn(ng, (K + nchunk - 1) / nchunk);
     int rc;
     for (int i = 0; i < ng; i++)
         if ((rc = jobs[i]->setup(kn[i]))) return rc;   // setup may shorten kn (grid limits)

@@ -377,6 +377,9 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Pe
     // tred[a], and the last of them adds the six totals to the step's slots in FP64
     __shared__ double tred[2][6];
     __shared__ int tcnt[2];
+    // the fused contraction's m(0) values of each epilogue warp's columns of the current tile
+    // (complex columns, nine vectors), staged once per tile
+    __shared__ __align__(16) float msm[PEW][9][QN / 4];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 1) {
@@ -503,6 +506,20 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Pe
             if (g.epilogue == 1 && r < g.M) sincosf(g.w[(size_t)bz * g.wstride + r] * g.dt_over_hbar, &sph, &cph);
             __nv_bfloat16 *Ch = g.Chi + (size_t)bz * g.sC, *Cl = g.Clo + (size_t)bz * g.sC;
             const float *m0p = fuse ? g.tcf_m0 + (size_t)bz * g.tcf_sm0 : nullptr;
+            float *mw = &msm[warp - 2][0][0];
+            if (fuse) {   // all of this warp's m(0) values for the tile in one round of loads
+                const int qb = (n0 + cbeg) >> 1;
+                __syncwarp();                     // the previous tile's reads are done
+                #pragma unroll
+                for (int b9 = 0; b9 < 9; b9++) {
+                    #pragma unroll
+                    for (int u = lane; u < QN / 4; u += 32) {
+                        const int q = qb + u;
+                        mw[b9 * (QN / 4) + u] = 2 * q + 1 < g.N ? __ldg(m0p + (size_t)b9 * g.tcf_ldv + q) : 0.f;
+                    }
+                }
+                __syncwarp();
+            }
             // epilogue 2 loads its row's D chunk one chunk ahead (hi and lo as four 16-byte words)
             const bool dpre = g.epilogue == 2 && r < g.M;
             auto dload = [&](int cc, uint4 *dd) -> bool {
@@ -604,21 +621,12 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Pe
                     }
                 }
                 if (fuse) {   // psi_a[r] += F'[r][q] m_a(0)[q] over the chunk's 8 complex columns
-                    const int q0 = c >> 1;
-                    const bool whole = 2 * (q0 + 8) <= g.N && (((uintptr_t)(m0p + q0) | ((size_t)g.tcf_ldv * 4)) & 15) == 0;
+                    const float *mc = mw + ((c0 - cbeg) >> 1);   // zero past the last column
                     #pragma unroll
                     for (int b9 = 0; b9 < 9; b9++) {
-                        float m[8];
-                        if (whole) {   // the chunk's 8 values of m_a(0) as two 16-byte loads
-                            const float4 x = __ldg(reinterpret_cast<const float4 *>(m0p + (size_t)b9 * g.tcf_ldv + q0));
-                            const float4 y = __ldg(reinterpret_cast<const float4 *>(m0p + (size_t)b9 * g.tcf_ldv + q0 + 4));
-                            m[0] = x.x; m[1] = x.y; m[2] = x.z; m[3] = x.w;
-                            m[4] = y.x; m[5] = y.y; m[6] = y.z; m[7] = y.w;
-                        } else {
-                            #pragma unroll
-                            for (int u = 0; u < 8; u++)
-                                m[u] = 2 * (q0 + u) + 1 < g.N ? __ldg(m0p + (size_t)b9 * g.tcf_ldv + q0 + u) : 0.f;
-                        }
+                        const float4 x = *reinterpret_cast<const float4 *>(mc + b9 * (QN / 4));
+                        const float4 y = *reinterpret_cast<const float4 *>(mc + b9 * (QN / 4) + 4);
+                        const float m[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
                         #pragma unroll
                         for (int u = 0; u < 8; u++) {
                             pr[b9] = fmaf(v[2 * u], m[u], pr[b9]);

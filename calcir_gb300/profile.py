@@ -6,6 +6,7 @@ CIR_EIGH_PROFILE=1 for the eigensolver's per-phase timers).
     python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 250
     python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 50 --propagate-vectors 1
     python -m calcir_gb300.profile grad --nmol 256 --nsamples 2 --ntcf 32
+    python -m calcir_gb300.profile noalloc --nmol 256 --batch 16
 
 Every stage goes through the C ABI (libcalcir.so)."""
 from __future__ import annotations
@@ -53,6 +54,24 @@ def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32", **options)
         print(f"run nmol {nmol}: {out['frame_steps_per_s']:.1f} frame-steps/s", eng.stats(), flush=True)
 
 
+def noalloc(nmol: int, nb: int) -> None:
+    """cir_eigh_noalloc on device copies of water Hamiltonians (the implicit-QR eigensolver
+    path: k_eigh_tq, k_eigh_formq, k_eigh_qr)."""
+    import ctypes as C
+    import torch
+    from calcir_gb300._lib import check, load
+    xyz, box = cg.synth_trajectory(nmol, 8, seed=3)
+    p = cg.default_params(model="tip4p2005", species="H2O", avef=3415.0)
+    with cg.Engine(p, xyz.shape[1]) as eng:
+        H, _, _, _ = eng.build_hamiltonian(xyz, box)
+    n = H.shape[-1]
+    A = torch.from_numpy(np.ascontiguousarray(H[np.arange(nb) % 8])).cuda()
+    w = torch.empty((nb, n), dtype=torch.float32, device="cuda")
+    check(load().cir_eigh_noalloc(nb, n, C.c_void_p(A.data_ptr()), C.c_void_p(w.data_ptr()), None))
+    torch.cuda.synchronize()
+    print(f"noalloc eigh N={n} batch {nb}: lowest eigenvalue {w.min().item():.2f}", flush=True)
+
+
 def grad(nmol: int, nsamples: int, ntcf: int) -> None:
     """One loss + gradient evaluation (cir_loss_grad): the adjoint kernels."""
     p = cg.default_params(model="tip4p2005", species="H2O", ntcfpoints=ntcf, nsamples=nsamples, sampleEvery=2.0,
@@ -83,6 +102,9 @@ def main() -> None:
     r.add_argument("--autotune", type=int, default=1)
     for opt in ("propagate-vectors", "share-frames", "refine-eigen"):
         r.add_argument("--" + opt, type=int, default=0)
+    na = sub.add_parser("noalloc")
+    na.add_argument("--nmol", type=int, default=256)
+    na.add_argument("--batch", type=int, default=16)
     gr = sub.add_parser("grad")
     gr.add_argument("--nmol", type=int, default=256)
     gr.add_argument("--nsamples", type=int, default=2)
@@ -94,6 +116,8 @@ def main() -> None:
         prop(a.n, a.nprop, a.precision)
     elif a.cmd == "grad":
         grad(a.nmol, a.nsamples, a.ntcf)
+    elif a.cmd == "noalloc":
+        noalloc(a.nmol, a.batch)
     else:
         run(a.nmol, a.nsamples, a.ntcf, a.precision, propagate_vectors=a.propagate_vectors,
             share_frames=a.share_frames, refine_eigen=a.refine_eigen, autotune=a.autotune)
