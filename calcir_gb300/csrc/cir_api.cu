@@ -1095,6 +1095,7 @@ struct GroupJob {
             c->stats.ms_eig += x;
             cudaEventElapsedTime(&x, ev[2], ev[5]);
             c->stats.ms_tridiag += x;
+            if (p.verbose > 1) printf("  order %d, steps %d..%d: tridiagonalisation %.1f ms\n", n, k0, k0 + kc - 1, x);
         }
         return CIR_OK;
     }
@@ -1317,6 +1318,8 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
     GroupJob j(c, c->buf, g, dxyz, dbox, fidx, res);
     int rc;
     if ((rc = j.setup(0))) return rc;
+    if (c->p.verbose > 1)
+        printf("group of %d chromophores: %d origins, chunks of %d steps\n", j.n, j.St, j.kn);
     cudaEvent_t *ev = c->ev;
     CK(cudaEventRecord(ev[0], c->stream));
     for (int k0 = 0; k0 < j.K; k0 += j.kn) {
@@ -1331,6 +1334,7 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         c->stats.ms_eig += x;
         cudaEventElapsedTime(&x, ev[2], ev[5]);
         c->stats.ms_tridiag += x;
+        if (c->p.verbose > 1) printf("  order %d, steps %d..%d: tridiagonalisation %.1f ms\n", j.n, k0, k0 + j.kc - 1, x);
         cudaEventElapsedTime(&x, ev[3], ev[4]);
         c->stats.ms_prop += x;
     }
@@ -1390,8 +1394,12 @@ static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &
         if (total <= budget) break;
     }
     int rc;
-    for (int i = 0; i < ng; i++)
+    for (int i = 0; i < ng; i++) {
         if ((rc = jobs[i]->setup(kn[i]))) return rc;   // setup may shorten kn (grid limits)
+        if (p.verbose)
+            printf("joint group of %d chromophores: %d origins, chunks of %d steps\n", jobs[i]->n, jobs[i]->St,
+                   jobs[i]->kn);
+    }
     cudaEvent_t *ev = c->ev;
     int launches = 0;
     std::vector<int> next(ng, 0);   // first step not covered by each group's prepared chunk
