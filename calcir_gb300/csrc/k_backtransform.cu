@@ -19,6 +19,9 @@
 // T[j][j] = tau_j, and Y_b into rows kb.. of Z (Y[kb+j][r] for r >= kb).
 #include "cir_device.cuh"
 
+#include <cstdlib>
+#include <vector>
+
 namespace {
 
 constexpr int BT_NB = 128;              // reflectors per block
@@ -261,7 +264,98 @@ __global__ void __launch_bounds__(256) k_bt_split_q(const float *Q, long long sQ
     }
 }
 
+// The split form's preparation on tensor cores, in four launches instead of k_bt_prep<1>:
+//   k_bt_clean  V_b with its implied zeros and unit as a split pair in two layouts: columns
+//               (the product P = Z^T V_b and G read it K-major over rows) and rows (the
+//               block's Y_b^T region, which the product Y_b^T = V_b T reads K-major over
+//               reflectors and then overwrites in place)
+//   G_b = V_b^T V_b on the persistent split-BF16 GEMM (FP32 out)
+//   k_bt_tmat   T by the slarft recursion from G_b and tau, stored transposed as a pair
+//   Y_b^T = V_b T on the persistent GEMM, in place over V_b's row layout
+// One thread block per reflector block and matrix: rows kb.. in chunks of BT_RC staged
+// like k_bt_prep's, written as pairs column-wise and, transposed through shared memory,
+// row-wise (columns j >= nbb of the row layout are zero).
+__global__ void __launch_bounds__(BT_NT) k_bt_clean(EighArgs a, BtSplit sp) {
+    extern __shared__ __align__(16) float bsm[];
+    float *Vt = bsm;                          // [BT_NB][BT_LDV]
+    const int n = a.n, ld = a.ld, mat = blockIdx.y;
+    const int kb = blockIdx.x * BT_NB, nbb = min(BT_NB, n - 2 - kb);
+    float *A = a.A + (size_t)mat * a.mstride;
+    const size_t ov = (size_t)mat * sp.sV;
+    const size_t oy = (size_t)mat * sp.sY + bt_yoff(blockIdx.x, n, sp.ldy);
+    const int t = threadIdx.x;
+    for (int r0 = kb; r0 < n; r0 += BT_RC) {
+        __syncthreads();
+        bt_stage(A, ld, n, kb, nbb, r0, false, Vt);
+        __syncthreads();
+        for (int idx = t; idx < BT_NB * BT_RC; idx += BT_NT) {   // column layout, rows contiguous
+            const int j = idx / BT_RC, rr = idx - j * BT_RC, r = r0 + rr;
+            if (j < nbb && r < n) {
+                const float x = Vt[j * BT_LDV + rr];
+                const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                const size_t o = ov + (size_t)(kb + j) * sp.ldq + r;
+                sp.V.hi[o] = h;
+                sp.V.lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+            }
+        }
+        for (int idx = t; idx < BT_RC * sp.ldy; idx += BT_NT) {  // row layout, reflectors contiguous
+            const int rr = idx / sp.ldy, j = idx - rr * sp.ldy, r = r0 + rr;
+            if (r < n) {
+                const float x = j < nbb ? Vt[j * BT_LDV + rr] : 0.f;
+                const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                const size_t o = oy + (size_t)(r - kb) * sp.ldy + j;
+                sp.Yt.hi[o] = h;
+                sp.Yt.lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+            }
+        }
+    }
+}
+
+// T of one reflector block (LAPACK slarft, forward, columnwise) from G = V_b^T V_b (FP32,
+// row-major BT_NB x BT_NB at Gb) and tau: T[i][j] = -tau_j sum_{i <= l < j} T[i][l] G[l][j],
+// T[j][j] = tau_j; written transposed as a pair, Tt[j*BT_NB + i] = T[i][j] (zero for i > j
+// and for rows or columns past the block's reflectors).
+__global__ void __launch_bounds__(BT_NB) k_bt_tmat(EighArgs a, const float *Gb, SplitMat Tt, long long sG,
+                                                  long long sT) {
+    extern __shared__ __align__(16) float bsm[];
+    float *M = bsm;                           // [BT_NB][BT_LDM]: G above the diagonal, T^T below
+    float *tau = M + BT_NB * BT_LDM;          // [BT_NB]
+    const int n = a.n, ld = a.ld, mat = blockIdx.y, b = blockIdx.x;
+    const int kb = b * BT_NB, nbb = min(BT_NB, n - 2 - kb);
+    const float *G = Gb + (size_t)mat * sG + (size_t)b * BT_NB * BT_NB;
+    const int t = threadIdx.x;
+    tau[t] = t < nbb ? a.DE[(size_t)mat * 3 * ld + 2 * ld + kb + t] : 0.f;
+    for (int l = 0; l < BT_NB; l++) M[l * BT_LDM + t] = (l < nbb && t < nbb) ? G[(size_t)l * BT_NB + t] : 0.f;
+    __syncthreads();
+    for (int j = 0; j < BT_NB; j++) {
+        if (t < j) {
+            float s = 0.f;
+            for (int l = t; l < j; l++) s = fmaf(M[l * BT_LDM + t], M[l * BT_LDM + j], s);
+            M[j * BT_LDM + t] = -tau[j] * s;
+        } else if (t == j) {
+            M[j * BT_LDM + j] = tau[j];
+        }
+        __syncthreads();
+    }
+    const size_t o = (size_t)mat * sT + (size_t)b * BT_NB * BT_NB;
+    for (int j = 0; j < BT_NB; j++) {   // thread t writes Tt[j][t] = T[t][j]: row j, contiguous in t
+        const float x = t <= j ? M[j * BT_LDM + t] : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        Tt.hi[o + (size_t)j * BT_NB + t] = h;
+        Tt.lo[o + (size_t)j * BT_NB + t] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+}
+
 }  // namespace
+
+// CIR_BT_TC=0: the split form's preparation in the one SIMT kernel k_bt_prep<1> (for comparison)
+static bool bt_tc_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_BT_TC");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 
 // The mixed forms with ld a multiple of 8: every operand as a BF16 split pair and the
 // products on the pre-split tensor-core GEMM (k_tc_split.cu).  Q is first split into Qs
@@ -279,14 +373,64 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
     k_bt_split_q<<<dim3((n + BT_SQ_ROWS - 1) / BT_SQ_ROWS, nmat), 256, 0, s>>>(Q, ms, n, ld, Qs, ss);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const size_t smem = bt_prep_smem();
-    if ((e = cudaFuncSetAttribute(k_bt_prep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-        return e;
     const int bw = min(BT_NB, (nrefl + 7) & ~7);   // width of P and of the Y_b^T blocks (<= ld)
     BtSplit sp{Vs, Ys, ld, bw, ss, ss};
-    k_bt_prep<true><<<dim3(nblk, nmat), BT_NT, smem, s>>>(a, sp);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    nl += 2;
+    nl += 1;
+    if (bt_tc_enabled() && bw == BT_NB && (long long)nblk * 2 * BT_NB * BT_NB <= ms) {
+        // the preparation on tensor cores: V_b in both layouts, G_b = V_b^T V_b, T, Y_b^T = V_b T.
+        // G_b (FP32) and T^T (a pair) live in U, which the products P only need afterwards.
+        float *Gb = U;                                              // [nblk][BT_NB][BT_NB] per matrix
+        const SplitMat Tt{reinterpret_cast<__nv_bfloat16 *>(U + (size_t)nblk * BT_NB * BT_NB),
+                          reinterpret_cast<__nv_bfloat16 *>(U + (size_t)nblk * BT_NB * BT_NB) + (size_t)nblk * BT_NB * BT_NB};
+        const size_t csm = sizeof(float) * (size_t)BT_NB * BT_LDV;
+        k_bt_clean<<<dim3(nblk, nmat), BT_NT, csm, s>>>(a, sp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        std::vector<SplitGemmArgs> gs(nblk), ys(nblk);
+        std::vector<int> batch(nblk, nmat);
+        for (int b = 0; b < nblk; b++) {
+            const int kb = b * BT_NB, nbb = min(BT_NB, nrefl - kb), m = n - kb;
+            SplitGemmArgs &g = gs[b];                               // G_b = V_b^T V_b
+            g = SplitGemmArgs{};
+            g.Ahi = g.Bhi = Vs.hi + (size_t)kb * ld + kb; g.Alo = g.Blo = Vs.lo + (size_t)kb * ld + kb;
+            g.lda = g.ldb = ld; g.sA = g.sB = ss;
+            g.Cf = Gb + (size_t)b * BT_NB * BT_NB; g.ldc = BT_NB; g.sC = ms; g.out_mode = 2;
+            g.M = g.N = nbb; g.K = m;
+            g.err = a.err;
+            g.test_stall = a.test_stall;
+            g.tile_n = 128;
+            SplitGemmArgs &y = ys[b];                               // Y_b^T = V_b T, over V_b's row layout
+            y = SplitGemmArgs{};
+            y.Ahi = Ys.hi + bt_yoff(b, n, bw); y.Alo = Ys.lo + bt_yoff(b, n, bw); y.lda = bw; y.sA = ss;
+            y.Bhi = Tt.hi + (size_t)b * BT_NB * BT_NB; y.Blo = Tt.lo + (size_t)b * BT_NB * BT_NB; y.ldb = BT_NB; y.sB = ss;
+            y.Chi = Ys.hi + bt_yoff(b, n, bw); y.Clo = Ys.lo + bt_yoff(b, n, bw); y.ldc = bw; y.sC = ss; y.out_mode = 1;
+            y.M = m; y.N = nbb; y.K = nbb;
+            y.err = a.err;
+            y.test_stall = a.test_stall;
+            y.tile_n = 128;   // one tile spans every column: a tile's rows are read before it writes them
+        }
+        for (int b0 = 0; b0 < nblk; b0 += CIR_SPLIT_MAXP) {
+            const int np = min(CIR_SPLIT_MAXP, nblk - b0);
+            if ((e = cir_launch_split_gemm_multi(gs.data() + b0, batch.data() + b0, np, s, &nl)) != cudaSuccess) return e;
+        }
+        const size_t tsm = sizeof(float) * ((size_t)BT_NB * BT_LDM + BT_NB);
+        if ((e = cudaFuncSetAttribute(k_bt_tmat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm)) != cudaSuccess)
+            return e;
+        k_bt_tmat<<<dim3(nblk, nmat), BT_NB, tsm, s>>>(a, Gb, Tt, ms, ss);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        nl += 2;
+        for (int b0 = 0; b0 < nblk; b0 += CIR_SPLIT_MAXP) {
+            const int np = min(CIR_SPLIT_MAXP, nblk - b0);
+            if ((e = cir_launch_split_gemm_multi(ys.data() + b0, batch.data() + b0, np, s, &nl)) != cudaSuccess) return e;
+        }
+    } else {
+        const size_t smem = bt_prep_smem();
+        if ((e = cudaFuncSetAttribute(k_bt_prep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess)
+            return e;
+        k_bt_prep<true><<<dim3(nblk, nmat), BT_NT, smem, s>>>(a, sp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        nl += 1;
+    }
     for (int b = nblk - 1; b >= 0; b--) {
         const int kb = b * BT_NB, nbb = min(BT_NB, nrefl - kb), m = n - kb;
         SplitGemmArgs g1{};                                        // P = Z^T[:, kb:] V_b
