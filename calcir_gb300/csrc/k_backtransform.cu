@@ -79,6 +79,13 @@ __host__ __device__ inline long long bt_yoff(int b, int n, int ldy) {
     return (long long)ldy * ((long long)b * n - (long long)BT_NB * b * (b - 1) / 2);
 }
 
+// The paired layout (blocks 2q and 2q+1 applied as one block of 2*BT_NB reflectors): pair q's
+// Y^T is (n - 2*BT_NB*q) x (2*BT_NB), row-major, from row 2*BT_NB*q; block 2q fills its left
+// half, block 2q+1 its right half (zero in the first BT_NB rows, above its reflectors)
+__host__ __device__ inline long long bt_yoff2(int q, int n) {
+    return 2LL * BT_NB * ((long long)q * n - 2LL * BT_NB * q * (q - 1) / 2);
+}
+
 template <bool SPLIT>
 __global__ void __launch_bounds__(BT_NT, 2) k_bt_prep(EighArgs a, BtSplit sp) {
     extern __shared__ __align__(16) float bsm[];
@@ -275,16 +282,21 @@ __global__ void __launch_bounds__(256) k_bt_split_q(const float *Q, long long sQ
 // One thread block per reflector block and matrix: rows kb.. in chunks of BT_RC staged
 // like k_bt_prep's, written as pairs column-wise and, transposed through shared memory,
 // row-wise (columns j >= nbb of the row layout are zero).
+// PAIRED: the row layout in the paired form (bt_yoff2), and both layouts from the pair's first
+// row, so that the second block's columns hold zeros above its reflectors.
+template <bool PAIRED>
 __global__ void __launch_bounds__(BT_NT) k_bt_clean(EighArgs a, BtSplit sp) {
     extern __shared__ __align__(16) float bsm[];
     float *Vt = bsm;                          // [BT_NB][BT_LDV]
-    const int n = a.n, ld = a.ld, mat = blockIdx.y;
-    const int kb = blockIdx.x * BT_NB, nbb = min(BT_NB, n - 2 - kb);
+    const int n = a.n, ld = a.ld, mat = blockIdx.y, b = blockIdx.x;
+    const int kb = b * BT_NB, nbb = min(BT_NB, n - 2 - kb);
+    const int rs = PAIRED ? (b & ~1) * BT_NB : kb;         // first row written
+    const int ldy = PAIRED ? 2 * BT_NB : sp.ldy, wy = PAIRED ? BT_NB : sp.ldy;   // row stride, columns
     float *A = a.A + (size_t)mat * a.mstride;
     const size_t ov = (size_t)mat * sp.sV;
-    const size_t oy = (size_t)mat * sp.sY + bt_yoff(blockIdx.x, n, sp.ldy);
+    const size_t oy = (size_t)mat * sp.sY + (PAIRED ? bt_yoff2(b >> 1, n) + (b & 1) * BT_NB : bt_yoff(b, n, sp.ldy));
     const int t = threadIdx.x;
-    for (int r0 = kb; r0 < n; r0 += BT_RC) {
+    for (int r0 = rs; r0 < n; r0 += BT_RC) {
         __syncthreads();
         bt_stage(A, ld, n, kb, nbb, r0, false, Vt);
         __syncthreads();
@@ -298,12 +310,12 @@ __global__ void __launch_bounds__(BT_NT) k_bt_clean(EighArgs a, BtSplit sp) {
                 sp.V.lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
             }
         }
-        for (int idx = t; idx < BT_RC * sp.ldy; idx += BT_NT) {  // row layout, reflectors contiguous
-            const int rr = idx / sp.ldy, j = idx - rr * sp.ldy, r = r0 + rr;
+        for (int idx = t; idx < BT_RC * wy; idx += BT_NT) {  // row layout, reflectors contiguous
+            const int rr = idx / wy, j = idx - rr * wy, r = r0 + rr;
             if (r < n) {
                 const float x = j < nbb ? Vt[j * BT_LDV + rr] : 0.f;
                 const __nv_bfloat16 h = __float2bfloat16_rn(x);
-                const size_t o = oy + (size_t)(r - kb) * sp.ldy + j;
+                const size_t o = oy + (size_t)(r - rs) * ldy + j;
                 sp.Yt.hi[o] = h;
                 sp.Yt.lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
             }
@@ -346,6 +358,57 @@ __global__ void __launch_bounds__(BT_NB) k_bt_tmat(EighArgs a, const float *Gb, 
     }
 }
 
+// Pair q of reflector blocks (b1 = 2q, b2 = 2q + 1) applied as one block: with X = V_2^T V_1,
+// T = [[T_1, -T_1 X^T T_2], [0, T_2]] and Y = T^T V^T = [Y_1; Y_2 - C Y_1], C = T_2^T X.
+// k_bt_cross forms C (X in FP32 at X + q*BT_NB^2, row-major; T_2 from its pair in Tt) and
+// writes it as a pair, row-major, at Cs + q*BT_NB^2.  Thread t computes column t % BT_NB of
+// rows 64 (t / BT_NB) .. +63; X is masked to the blocks' nbb2 x nbb1 part, T_2 holds zeros
+// outside its triangle.
+constexpr int BT_CX_NT = 2 * BT_NB;
+constexpr int BT_CX_LDT = BT_NB + 4;
+constexpr size_t bt_cross_smem() { return sizeof(float) * ((size_t)BT_NB * BT_CX_LDT + (size_t)BT_NB * BT_NB); }
+
+__global__ void __launch_bounds__(BT_CX_NT) k_bt_cross(EighArgs a, const float *X, SplitMat Tt, SplitMat Cs,
+                                                      long long sX, long long sT) {
+    extern __shared__ __align__(16) float bsm[];
+    float *Ts = bsm;                          // Ts[l][i] = T_2[l][i]
+    float *Xs = Ts + BT_NB * BT_CX_LDT;       // Xs[l][j] = X[l][j]
+    const int q = blockIdx.x, mat = blockIdx.y, t = threadIdx.x, nrefl = a.n - 2;
+    const int nbb1 = min(BT_NB, nrefl - 2 * q * BT_NB), nbb2 = min(BT_NB, nrefl - (2 * q + 1) * BT_NB);
+    const float *Xg = X + (size_t)mat * sX + (size_t)q * BT_NB * BT_NB;
+    const size_t to = (size_t)mat * sT + (size_t)(2 * q + 1) * BT_NB * BT_NB;
+    for (int idx = t; idx < BT_NB * BT_NB; idx += BT_CX_NT) {
+        const int r = idx / BT_NB, c = idx - r * BT_NB;   // Tt[r*BT_NB + c] = T_2[c][r]
+        Ts[c * BT_CX_LDT + r] = __bfloat162float(Tt.hi[to + idx]) + __bfloat162float(Tt.lo[to + idx]);
+        Xs[idx] = (r < nbb2 && c < nbb1) ? Xg[idx] : 0.f;
+    }
+    __syncthreads();
+    const int j = t % BT_NB, i0 = 64 * (t / BT_NB);
+    float acc[64];
+    #pragma unroll
+    for (int i = 0; i < 64; i++) acc[i] = 0.f;
+    #pragma unroll 2
+    for (int l = 0; l < BT_NB; l++) {
+        const float x = Xs[l * BT_NB + j];
+        const float4 *tr = reinterpret_cast<const float4 *>(Ts + l * BT_CX_LDT + i0);
+        #pragma unroll
+        for (int i4 = 0; i4 < 16; i4++) {
+            const float4 tv = tr[i4];
+            acc[4 * i4] = fmaf(tv.x, x, acc[4 * i4]);
+            acc[4 * i4 + 1] = fmaf(tv.y, x, acc[4 * i4 + 1]);
+            acc[4 * i4 + 2] = fmaf(tv.z, x, acc[4 * i4 + 2]);
+            acc[4 * i4 + 3] = fmaf(tv.w, x, acc[4 * i4 + 3]);
+        }
+    }
+    const size_t oc = (size_t)mat * sT + (size_t)q * BT_NB * BT_NB;
+    #pragma unroll
+    for (int i = 0; i < 64; i++) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(acc[i]);
+        Cs.hi[oc + (size_t)(i0 + i) * BT_NB + j] = h;
+        Cs.lo[oc + (size_t)(i0 + i) * BT_NB + j] = __float2bfloat16_rn(acc[i] - __bfloat162float(h));
+    }
+}
+
 }  // namespace
 
 // CIR_BT_TC=0: the split form's preparation in the one SIMT kernel k_bt_prep<1> (for comparison)
@@ -355,6 +418,146 @@ static bool bt_tc_enabled() {
         return !(v && v[0] == '0');
     }();
     return on;
+}
+
+// CIR_BT_PAIR=0: blocks of BT_NB reflectors in the split form's updates, not pairs of them
+static bool bt_pair_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_BT_PAIR");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+static cudaError_t multi_gemm(std::vector<SplitGemmArgs> &g, int nmat, cudaStream_t s, int &nl) {
+    std::vector<int> batch(g.size(), nmat);
+    for (size_t i = 0; i < g.size(); i += CIR_SPLIT_MAXP) {
+        const int np = (int)std::min<size_t>(CIR_SPLIT_MAXP, g.size() - i);
+        const cudaError_t e = cir_launch_split_gemm_multi(g.data() + i, batch.data() + i, np, s, &nl);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// The split form in pairs of reflector blocks: blocks 2q and 2q+1 are applied as one block of
+// 2*BT_NB reflectors (k_bt_cross), so Z is read and written half as often.  Per block as in
+// backtransform_split's single-block preparation (clean, G, T, Y_b^T = V_b T), the row layout
+// of V_b and so Y_b^T in the paired layout; then per pair X = V_2^T V_1, C = T_2^T X and the
+// second half of Y^T less Y_1^T C^T; then per pair from the last, P = Z^T[:, kq:] V_q and
+// Z^T[:, kq:] -= P Y_q.  G, T, X and C live in U, which the products P need only afterwards.
+// Returns cudaErrorNotSupported when the work areas do not fit (the caller falls back).
+static cudaError_t backtransform_paired(const EighArgs &a, const SplitMat &Qs, const SplitMat &Vs, const SplitMat &Ys,
+                                        float *U, int nmat, int nblk, cudaStream_t s, int &nl) {
+    const int n = a.n, ld = a.ld, nrefl = n - 2, npair = (nblk + 1) / 2, npf = nblk / 2;
+    const long long ms = a.mstride, ss = 2 * a.mstride, B2 = (long long)BT_NB * BT_NB;
+    if (nblk < 2 || ld < 2 * BT_NB || (2LL * nblk + 2LL * npf) * B2 > ms || bt_yoff2(npair, n) > ms ||
+        (long long)n * 2 * BT_NB > ms)
+        return cudaErrorNotSupported;
+    auto nbb = [&](int b) { return min(BT_NB, nrefl - b * BT_NB); };
+    float *Gb = U, *Xq = U + 2LL * nblk * B2;
+    __nv_bfloat16 *tb = reinterpret_cast<__nv_bfloat16 *>(U + (long long)nblk * B2);
+    __nv_bfloat16 *cb = reinterpret_cast<__nv_bfloat16 *>(U + (2LL * nblk + npf) * B2);
+    const SplitMat Tt{tb, tb + nblk * B2}, Cs{cb, cb + npf * B2};
+    const SplitMat Ps{reinterpret_cast<__nv_bfloat16 *>(U), reinterpret_cast<__nv_bfloat16 *>(U) + ms};
+    const int ldy = 2 * BT_NB;
+    auto yoff = [&](int b) { return bt_yoff2(b >> 1, n) + (b & 1) * BT_NB; };   // block b's row layout
+    auto base = [&](SplitGemmArgs &g) {
+        g = SplitGemmArgs{};
+        g.err = a.err;
+        g.test_stall = a.test_stall;
+        g.tile_n = 128;
+    };
+    cudaError_t e;
+    k_bt_clean<true><<<dim3(nblk, nmat), BT_NT, sizeof(float) * (size_t)BT_NB * BT_LDV, s>>>(
+        a, BtSplit{Vs, Ys, ld, ldy, ss, ss});
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    nl += 1;
+    std::vector<SplitGemmArgs> gx, ys, cr;
+    for (int b = 0; b < nblk; b++) {   // G_b = V_b^T V_b
+        const int kb = b * BT_NB;
+        SplitGemmArgs g;
+        base(g);
+        g.Ahi = g.Bhi = Vs.hi + (size_t)kb * ld + kb; g.Alo = g.Blo = Vs.lo + (size_t)kb * ld + kb;
+        g.lda = g.ldb = ld; g.sA = g.sB = ss;
+        g.Cf = Gb + (size_t)b * B2; g.ldc = BT_NB; g.sC = ms; g.out_mode = 2;
+        g.M = g.N = nbb(b); g.K = n - kb;
+        gx.push_back(g);
+    }
+    for (int q = 0; q < npf; q++) {    // X_q = V_2^T V_1 over the rows of V_2
+        const int k1 = 2 * q * BT_NB, k2 = k1 + BT_NB;
+        SplitGemmArgs g;
+        base(g);
+        g.Ahi = Vs.hi + (size_t)k2 * ld + k2; g.Alo = Vs.lo + (size_t)k2 * ld + k2; g.lda = ld; g.sA = ss;
+        g.Bhi = Vs.hi + (size_t)k1 * ld + k2; g.Blo = Vs.lo + (size_t)k1 * ld + k2; g.ldb = ld; g.sB = ss;
+        g.Cf = Xq + (size_t)q * B2; g.ldc = BT_NB; g.sC = ms; g.out_mode = 2;
+        g.M = nbb(2 * q + 1); g.N = nbb(2 * q); g.K = n - k2;
+        gx.push_back(g);
+    }
+    if ((e = multi_gemm(gx, nmat, s, nl)) != cudaSuccess) return e;
+    const size_t tsm = sizeof(float) * ((size_t)BT_NB * BT_LDM + BT_NB);
+    if ((e = cudaFuncSetAttribute(k_bt_tmat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm)) != cudaSuccess)
+        return e;
+    k_bt_tmat<<<dim3(nblk, nmat), BT_NB, tsm, s>>>(a, Gb, Tt, ms, ss);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    nl += 1;
+    if (npf > 0) {
+        if ((e = cudaFuncSetAttribute(k_bt_cross, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt_cross_smem())) !=
+            cudaSuccess)
+            return e;
+        k_bt_cross<<<dim3(npf, nmat), BT_CX_NT, bt_cross_smem(), s>>>(a, Xq, Tt, Cs, ms, ss);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        nl += 1;
+    }
+    for (int b = 0; b < nblk; b++) {   // Y_b^T = V_b T_b in place over V_b's row layout
+        const int rs = (b & ~1) * BT_NB;
+        SplitGemmArgs y;
+        base(y);   // 128-wide tiles span every column: a tile's rows are read before it writes them
+        y.Ahi = y.Chi = Ys.hi + yoff(b); y.Alo = y.Clo = Ys.lo + yoff(b); y.lda = y.ldc = ldy; y.sA = y.sC = ss;
+        y.Bhi = Tt.hi + (size_t)b * B2; y.Blo = Tt.lo + (size_t)b * B2; y.ldb = BT_NB; y.sB = ss;
+        y.out_mode = 1;
+        y.M = n - rs; y.N = y.K = nbb(b);
+        ys.push_back(y);
+    }
+    if ((e = multi_gemm(ys, nmat, s, nl)) != cudaSuccess) return e;
+    for (int q = 0; q < npf; q++) {    // Y_2^T -= Y_1^T C^T, in place (the right half of the pair's rows)
+        SplitGemmArgs g;
+        base(g);
+        const long long o = bt_yoff2(q, n);
+        g.Ahi = Ys.hi + o; g.Alo = Ys.lo + o; g.lda = ldy; g.sA = ss;
+        g.Bhi = Cs.hi + (size_t)q * B2; g.Blo = Cs.lo + (size_t)q * B2; g.ldb = BT_NB; g.sB = ss;
+        g.epilogue = 2;
+        g.Dhi = g.Chi = Ys.hi + o + BT_NB; g.Dlo = g.Clo = Ys.lo + o + BT_NB; g.ldd = g.ldc = ldy; g.sD = g.sC = ss;
+        g.out_mode = 1;
+        g.M = n - 2 * q * BT_NB; g.N = nbb(2 * q + 1); g.K = nbb(2 * q);
+        cr.push_back(g);
+    }
+    if ((e = multi_gemm(cr, nmat, s, nl)) != cudaSuccess) return e;
+    for (int q = npair - 1; q >= 0; q--) {
+        const int kq = 2 * q * BT_NB, m = n - kq, wq = nbb(2 * q) + (2 * q + 1 < nblk ? nbb(2 * q + 1) : 0);
+        SplitGemmArgs g1;                                          // P = Z^T[:, kq:] V_q
+        base(g1);
+        g1.tile_n = 0;
+        g1.Ahi = Qs.hi + kq; g1.Alo = Qs.lo + kq; g1.lda = ld; g1.sA = ss;
+        g1.Bhi = Vs.hi + (size_t)kq * ld + kq; g1.Blo = Vs.lo + (size_t)kq * ld + kq; g1.ldb = ld; g1.sB = ss;
+        g1.Chi = Ps.hi; g1.Clo = Ps.lo; g1.ldc = ldy; g1.sC = ss; g1.out_mode = 1;
+        g1.M = n; g1.N = wq; g1.K = m;
+        SplitGemmArgs g2;                                          // Z^T[:, kq:] -= P Y_q
+        base(g2);
+        g2.tile_n = 0;
+        g2.Ahi = Ps.hi; g2.Alo = Ps.lo; g2.lda = ldy; g2.sA = ss;
+        g2.Bhi = Ys.hi + bt_yoff2(q, n); g2.Blo = Ys.lo + bt_yoff2(q, n); g2.ldb = ldy; g2.sB = ss;
+        g2.epilogue = 2;
+        g2.Dhi = Qs.hi + kq; g2.Dlo = Qs.lo + kq; g2.ldd = ld; g2.sD = ss;
+        if (q > 0) {
+            g2.Chi = Qs.hi + kq; g2.Clo = Qs.lo + kq; g2.ldc = ld; g2.sC = ss; g2.out_mode = 1;
+        } else {
+            g2.Cf = a.A; g2.ldc = ld; g2.sC = ms; g2.out_mode = 2;
+        }
+        g2.M = n; g2.N = m; g2.K = wq;
+        if ((e = cir_launch_split_gemm(g1, nmat, s, &nl)) != cudaSuccess) return e;
+        if ((e = cir_launch_split_gemm(g2, nmat, s, &nl)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // The mixed forms with ld a multiple of 8: every operand as a BF16 split pair and the
@@ -376,6 +579,10 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
     const int bw = min(BT_NB, (nrefl + 7) & ~7);   // width of P and of the Y_b^T blocks (<= ld)
     BtSplit sp{Vs, Ys, ld, bw, ss, ss};
     nl += 1;
+    if (bt_tc_enabled() && bt_pair_enabled() && bw == BT_NB) {
+        e = backtransform_paired(a, Qs, Vs, Ys, U, nmat, nblk, s, nl);
+        if (e != cudaErrorNotSupported) return e;
+    }
     if (bt_tc_enabled() && bw == BT_NB && (long long)nblk * 2 * BT_NB * BT_NB <= ms) {
         // the preparation on tensor cores: V_b in both layouts, G_b = V_b^T V_b, T, Y_b^T = V_b T.
         // G_b (FP32) and T^T (a pair) live in U, which the products P only need afterwards.
@@ -383,7 +590,7 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
         const SplitMat Tt{reinterpret_cast<__nv_bfloat16 *>(U + (size_t)nblk * BT_NB * BT_NB),
                           reinterpret_cast<__nv_bfloat16 *>(U + (size_t)nblk * BT_NB * BT_NB) + (size_t)nblk * BT_NB * BT_NB};
         const size_t csm = sizeof(float) * (size_t)BT_NB * BT_LDV;
-        k_bt_clean<<<dim3(nblk, nmat), BT_NT, csm, s>>>(a, sp);
+        k_bt_clean<false><<<dim3(nblk, nmat), BT_NT, csm, s>>>(a, sp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         std::vector<SplitGemmArgs> gs(nblk), ys(nblk);
         std::vector<int> batch(nblk, nmat);
