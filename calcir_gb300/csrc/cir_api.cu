@@ -805,6 +805,42 @@ static std::vector<long long> step_key(const Group &g, int St, int K, int k0, in
 static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long long sV, const float *w, long long sw,
                          float dt, float *x, float *tmp, int &launches);
 
+// Thread blocks of the tridiagonalisation of order n resident at a time (one per matrix).
+static int tridiag_wave(cir_ctx *c, int n) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 1;
+    auto it = c->tq_blocks.find(n);
+    const int blocks = it != c->tq_blocks.end() && it->second > 0 ? it->second : cir_tridiag_blocks(n);
+    return std::max(1, sms * blocks);
+}
+
+// Chunk length for K steps of St origins, at most kn_max steps a chunk.  The
+// tridiagonalisation runs `wave` matrices at a time, and a chunk whose last wave is nearly
+// empty pays for about a third of a wave while its few blocks run alone (order 1024 at 456
+// resident blocks: 3232 matrices, 7.09 waves, 525 ms; 3168 matrices, 6.95 waves, 501 ms).
+// Of the chunkings into as few chunks as kn_max allows, equal in length but the last, the
+// one with the least estimated time is taken: whole waves, a part-filled last wave counted
+// as at least 0.3 of one; ties go to the longer chunks.
+static int plan_chunk(int K, int St, int kn_max, int wave) {
+    kn_max = std::max(1, std::min(kn_max, K));
+    const int nc = (K + kn_max - 1) / kn_max, kn_min = (K + nc - 1) / nc;
+    double best = 1e300;
+    int pick = kn_max;
+    for (int kn = kn_max; kn >= kn_min; kn--) {
+        double cost = 0.0;
+        for (int k0 = 0; k0 < K && cost < best; k0 += kn) {
+            const double w = (double)St * std::min(kn, K - k0) / wave, f = w - std::floor(w);
+            cost += std::floor(w) + (f > 0.0 ? std::max(f, 0.3) : 0.0);
+        }
+        if (cost < best - 1e-9) {
+            best = cost;
+            pick = kn;
+        }
+    }
+    return pick;
+}
+
 // One group's job: ntraj trajectories of one size, nsamples origins each, batched through
 // every launch.  dxyz / dbox hold all the group's frames on the device; fidx[(t*S + s)*K + k]
 // is the frame of step k of origin s of trajectory t; res[t] receives trajectory t's results.
@@ -815,6 +851,9 @@ static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long 
 struct GroupJob {
     cir_ctx *c;
     DevBuf *buf;
+    DevBuf *scr;   // the preparation's scratch (frames, tables, eigensolver work areas): buf, or
+                   // buffers that the groups of a joint run share, since their preparations
+                   // run one after another on the stream
     Group g;
     const float *dxyz, *dbox;
     const std::vector<int> &fidx;
@@ -834,12 +873,21 @@ struct GroupJob {
 
     GroupJob(cir_ctx *c_, DevBuf *buf_, const Group &g_, const float *dxyz_, const float *dbox_,
              const std::vector<int> &fidx_, cir_result *res_)
-        : c(c_), buf(buf_), g(g_), dxyz(dxyz_), dbox(dbox_), fidx(fidx_), res(res_), p(c_->p), ev(c_->ev) {}
+        : c(c_), buf(buf_), scr(buf_), g(g_), dxyz(dxyz_), dbox(dbox_), fidx(fidx_), res(res_), p(c_->p),
+          ev(c_->ev) {}
 
-    // bytes of device memory one origin-step of a chunk holds
+    // bytes of device memory one origin-step of a chunk holds from its preparation to the end
+    // of its step loop (V, the eigenvalues, dipoles and polarisabilities, the status) ...
+    static size_t resident_step_bytes(const cir_params &p, const Group &g) {
+        return (size_t)g.n * g.ld * 4 + (size_t)(9 + 1) * g.ld * 4 + 4;
+    }
+    // ... and during its preparation only (frames, tables, the eigensolver's work areas)
+    static size_t scratch_step_bytes(const cir_params &p, const Group &g) {
+        return (size_t)(p.refine_eigen > 0 ? 2 : 1) * g.n * g.ld * 4 + cir_dc_bytes(g.n, g.ld) + cir_eigh_de_bytes(g.ld) +
+               (size_t)CT_NROW * g.ld * 4 + (size_t)g.natoms * 12 + 60;
+    }
     static size_t per_step_bytes(const cir_params &p, const Group &g) {
-        return (size_t)(p.refine_eigen > 0 ? 3 : 2) * g.n * g.ld * 4 + cir_dc_bytes(g.n, g.ld) + cir_eigh_de_bytes(g.ld) +
-               (size_t)(9 + CT_NROW + 1) * g.ld * 4 + (size_t)g.natoms * 12 + 64;
+        return resident_step_bytes(p, g) + scratch_step_bytes(p, g);
     }
 
     // buffers, zeroed sums, tuned products; kn_set > 0 fixes the chunk length
@@ -854,24 +902,26 @@ struct GroupJob {
         size_t budget = (size_t)64 << 30;
         size_t freeb = 0, totalb = 0;
         if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget, freeb / 2);
-        kn = (int)std::max<size_t>(1, budget / (per_step * St));
+        kn = (int)std::min<size_t>((size_t)K, std::max<size_t>(1, budget / (per_step * St)));
+        kn = std::max(1, std::min(kn, 65535 / std::max(1, St)));   // matrices of a chunk index a grid dimension
+        kn = plan_chunk(K, St, kn, tridiag_wave(c, n));
         if (p.batch_frames > 0) kn = std::max(1, p.batch_frames / St);
         if (kn_set > 0) kn = kn_set;   // chosen by the caller for several groups together
         kn = std::min(kn, K);
-        kn = std::max(1, std::min(kn, 65535 / std::max(1, St)));   // matrices of a chunk index a grid dimension
+        kn = std::max(1, std::min(kn, 65535 / std::max(1, St)));
         if (St > 65535) return cir_fail(CIR_ERR_ARG, "%d time origins in one group (at most 65535)", St);
 
         CK(buf[B_FIDX].ensure((size_t)steps * 4));
         CK(cudaMemcpyAsync(buf[B_FIDX].p, fidx.data(), (size_t)steps * 4, cudaMemcpyHostToDevice, c->stream));
         nb = St * kn;
         mstride = (long long)n * ld;
-        CK(buf[B_CXYZ].ensure((size_t)nb * g.natoms * 12));
-        CK(buf[B_CBOX].ensure((size_t)nb * 12));
-        CK(buf[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
+        CK(scr[B_CXYZ].ensure((size_t)nb * g.natoms * 12));
+        CK(scr[B_CBOX].ensure((size_t)nb * 12));
+        CK(scr[B_CT].ensure((size_t)nb * CT_NROW * ld * 4));
         CK(buf[B_A].ensure((size_t)nb * mstride * 4));
-        CK(buf[B_Z].ensure((size_t)nb * mstride * 4));
-        CK(buf[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
-        CK(buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
+        CK(scr[B_Z].ensure((size_t)nb * mstride * 4));
+        CK(scr[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
+        CK(scr[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
         CK(buf[B_W].ensure((size_t)nb * ld * 4));
         CK(buf[B_M].ensure((size_t)nb * 9 * ld * 4));
         CK(buf[B_STATUS].ensure((size_t)nb * 4));
@@ -1004,16 +1054,16 @@ struct GroupJob {
         CK(cudaEventRecord(ev[1], c->stream));
         if (ufr)
             k_gather_frames<<<dim3(8, nmat), 256, 0, c->stream>>>(dxyz, dbox, ufr, g.natoms, 1, nmat, nmat, 0,
-                                                                  buf[B_CXYZ].as<float>(), buf[B_CBOX].as<float>());
+                                                                  scr[B_CXYZ].as<float>(), scr[B_CBOX].as<float>());
         else
             k_gather_frames<<<dim3(8, nbc), 256, 0, c->stream>>>(dxyz, dbox, buf[B_FIDX].as<int>(), g.natoms, St, kc,
-                                                                 K, k0, buf[B_CXYZ].as<float>(), buf[B_CBOX].as<float>());
+                                                                 K, k0, scr[B_CXYZ].as<float>(), scr[B_CBOX].as<float>());
         CK(cudaGetLastError());
         launches++;
         BuildArgs a = build_args(c, g);
-        a.xyz = buf[B_CXYZ].as<float>();
-        a.box = buf[B_CBOX].as<float>();
-        a.ct = buf[B_CT].as<float>();
+        a.xyz = scr[B_CXYZ].as<float>();
+        a.box = scr[B_CBOX].as<float>();
+        a.ct = scr[B_CT].as<float>();
         a.H = A;
         a.ldh = ld;
         a.dip = M;                    // frame b: M + b*9*ld, rows 0..2 dipole, 3..8 polarisability
@@ -1027,9 +1077,9 @@ struct GroupJob {
         memset(&e, 0, sizeof e);
         e.A = A;
         e.W = W;
-        e.Z = buf[B_Z].as<float>();
-        e.DC = buf[B_DC].as<float>();
-        e.DE = buf[B_DE].as<float>();
+        e.Z = scr[B_Z].as<float>();
+        e.DC = scr[B_DC].as<float>();
+        e.DE = scr[B_DE].as<float>();
         e.mstride = mstride;
         e.wstride = ld;
         e.n = n;
@@ -1367,31 +1417,40 @@ static bool joint_enabled() {
 static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &jobs) {
     const cir_params &p = c->p;
     const int K = p.ntcfpoints, ng = (int)jobs.size();
-    // chunk lengths: each group takes the chunks it would take alone (up to 64 GiB, balanced
-    // so that its chunks are of equal length and every eigensolver launch stays many waves
-    // long); the groups' chunks are resident together, so when their sum exceeds 60% of the
-    // free memory every group's share shrinks in proportion
+    // chunk lengths: each group takes the chunks it would take alone (up to 64 GiB, planned
+    // by plan_chunk against the tridiagonalisation's waves).  The groups' chunks are resident together, but only V, the eigenvalues and the
+    // dipoles stay from a preparation to the end of its step loop: the preparations run one
+    // after another and share one scratch (frames, tables, the eigensolver's work areas), so
+    // a run holds the sum of the resident parts and the largest scratch; when that exceeds
+    // 60% of the free memory every group's share shrinks in proportion
     size_t freeb = 0, totalb = 0;
     size_t budget = (size_t)64 << 30;
     if (cudaMemGetInfo(&freeb, &totalb) == cudaSuccess) budget = std::min(budget * ng, freeb / 10 * 6);
-    std::vector<size_t> per(ng);
-    for (int i = 0; i < ng; i++)
-        per[i] = GroupJob::per_step_bytes(p, jobs[i]->g) * (size_t)(p.nsamples * jobs[i]->g.ntraj);
+    std::vector<size_t> per(ng), res(ng), scr(ng);
+    for (int i = 0; i < ng; i++) {
+        const size_t st = (size_t)(p.nsamples * jobs[i]->g.ntraj);
+        per[i] = GroupJob::per_step_bytes(p, jobs[i]->g) * st;
+        res[i] = GroupJob::resident_step_bytes(p, jobs[i]->g) * st;
+        scr[i] = GroupJob::scratch_step_bytes(p, jobs[i]->g) * st;
+        jobs[i]->scr = c->buf;
+    }
     auto balanced = [&](double cap_bytes, int i) {
+        const int St = p.nsamples * jobs[i]->g.ntraj;
+        if (p.batch_frames > 0) return std::max(1, std::min(K, p.batch_frames / St));
         int km = (int)std::max(1.0, std::min((double)K, cap_bytes / (double)per[i]));
-        if (p.batch_frames > 0) km = std::max(1, std::min(K, p.batch_frames / (p.nsamples * jobs[i]->g.ntraj)));
-        const int nc = (K + km - 1) / km;
-        return (K + nc - 1) / nc;
+        km = std::max(1, std::min(km, 65535 / std::max(1, St)));
+        return plan_chunk(K, St, km, tridiag_wave(c, jobs[i]->g.n));
     };
     std::vector<int> kn(ng);
     double cap = (double)((size_t)64 << 30);
     for (int it = 0; it < 64; it++, cap *= 0.9) {
-        size_t total = 0;
+        size_t total = 0, smax = 0;
         for (int i = 0; i < ng; i++) {
             kn[i] = balanced(cap, i);
-            total += (size_t)kn[i] * per[i];
+            total += (size_t)kn[i] * res[i];
+            smax = std::max(smax, (size_t)kn[i] * scr[i]);
         }
-        if (total <= budget) break;
+        if (total + smax <= budget) break;
     }
     int rc;
     for (int i = 0; i < ng; i++) {
