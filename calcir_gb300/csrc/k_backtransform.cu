@@ -324,31 +324,77 @@ __global__ void __launch_bounds__(BT_NT) k_bt_clean(EighArgs a, BtSplit sp) {
 }
 
 // T of one reflector block (LAPACK slarft, forward, columnwise) from G = V_b^T V_b (FP32,
-// row-major BT_NB x BT_NB at Gb) and tau: T[i][j] = -tau_j sum_{i <= l < j} T[i][l] G[l][j],
-// T[j][j] = tau_j; written transposed as a pair, Tt[j*BT_NB + i] = T[i][j] (zero for i > j
-// and for rows or columns past the block's reflectors).
+// row-major BT_NB x BT_NB at Gb) and tau, written transposed as a pair, Tt[j*BT_NB + i] =
+// T[i][j] (zero for i > j and for rows or columns past the block's reflectors).  Blocked:
+// the four diagonal 32 x 32 blocks by the column recursion T[i][j] = -tau_j sum_{i <= l < j}
+// T[i][l] G[l][j], T[j][j] = tau_j (a warp each), then the blocks above them by
+// T_AB = -T_A G_AB T_B (the product of two compact-WY blocks), for the 32-column pairs (0,1),
+// (2,3) and then the 64-column halves; the same T, with the long dependent chains of the
+// plain recursion turned into products.  T[i][j] (i <= j) is kept at M[j][i], below the
+// diagonal, where G (read above the diagonal only) is no longer needed.
+constexpr size_t bt_tmat_smem() { return sizeof(float) * ((size_t)BT_NB * BT_LDM + BT_NB + 64 * 64); }
+
 __global__ void __launch_bounds__(BT_NB) k_bt_tmat(EighArgs a, const float *Gb, SplitMat Tt, long long sG,
                                                   long long sT) {
     extern __shared__ __align__(16) float bsm[];
     float *M = bsm;                           // [BT_NB][BT_LDM]: G above the diagonal, T^T below
     float *tau = M + BT_NB * BT_LDM;          // [BT_NB]
+    float *Ws = tau + BT_NB;                  // [64][64]: G_AB T_B
     const int n = a.n, ld = a.ld, mat = blockIdx.y, b = blockIdx.x;
     const int kb = b * BT_NB, nbb = min(BT_NB, n - 2 - kb);
     const float *G = Gb + (size_t)mat * sG + (size_t)b * BT_NB * BT_NB;
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     tau[t] = t < nbb ? a.DE[(size_t)mat * 3 * ld + 2 * ld + kb + t] : 0.f;
     for (int l = 0; l < BT_NB; l++) M[l * BT_LDM + t] = (l < nbb && t < nbb) ? G[(size_t)l * BT_NB + t] : 0.f;
     __syncthreads();
-    for (int j = 0; j < BT_NB; j++) {
-        if (t < j) {
-            float s = 0.f;
-            for (int l = t; l < j; l++) s = fmaf(M[l * BT_LDM + t], M[l * BT_LDM + j], s);
-            M[j * BT_LDM + t] = -tau[j] * s;
-        } else if (t == j) {
-            M[j * BT_LDM + j] = tau[j];
+    // the diagonal blocks: warp w, columns 32w + j, lane = row within the block
+    {
+        const int o = 32 * warp;
+        for (int j = 0; j < 32; j++) {
+            if (lane < j) {
+                float s = 0.f;
+                for (int l = lane; l < j; l++) s = fmaf(M[(o + l) * BT_LDM + o + lane], M[(o + l) * BT_LDM + o + j], s);
+                M[(o + j) * BT_LDM + o + lane] = -tau[o + j] * s;
+            } else if (lane == j) {
+                M[(o + j) * BT_LDM + o + j] = tau[o + j];
+            }
+            __syncwarp();
         }
-        __syncthreads();
     }
+    __syncthreads();
+    // T_AB = -T_A (G_AB T_B) for blocks A = [a0, a0 + w), B = [a0 + w, a0 + 2w); thread u of
+    // the NU threads on it computes column c = u % w of rows r0 .. r0 + R - 1, R = w*w / NU
+    auto combine = [&](int a0, int w, int u, int NU, float *W) {
+        constexpr int RMAX = 32;
+        const int R = w * w / NU, c = u % w, r0 = (u / w) * R, b0 = a0 + w;
+        float acc[RMAX];
+        #pragma unroll
+        for (int i = 0; i < RMAX; i++) acc[i] = 0.f;
+        for (int k = 0; k <= c; k++) {          // W = G_AB T_B, T_B upper triangular
+            const float tb = M[(b0 + c) * BT_LDM + b0 + k];
+            #pragma unroll
+            for (int i = 0; i < RMAX; i++)
+                if (i < R) acc[i] = fmaf(M[(a0 + r0 + i) * BT_LDM + b0 + k], tb, acc[i]);
+        }
+        #pragma unroll
+        for (int i = 0; i < RMAX; i++)
+            if (i < R) W[(r0 + i) * w + c] = acc[i];
+        __syncthreads();
+        #pragma unroll
+        for (int i = 0; i < RMAX; i++) acc[i] = 0.f;
+        for (int k = r0; k < w; k++) {          // T_AB = -T_A W, T_A upper triangular
+            const float wk = W[k * w + c];
+            #pragma unroll
+            for (int i = 0; i < RMAX; i++)
+                if (i < R && r0 + i <= k) acc[i] = fmaf(M[(a0 + k) * BT_LDM + a0 + r0 + i], wk, acc[i]);
+        }
+        #pragma unroll
+        for (int i = 0; i < RMAX; i++)
+            if (i < R) M[(b0 + c) * BT_LDM + a0 + r0 + i] = -acc[i];
+        __syncthreads();
+    };
+    combine(64 * (t >> 6), 32, t & 63, 64, Ws + (t >> 6) * 1024);   // pairs (0,1) and (2,3)
+    combine(0, 64, t, BT_NB, Ws);                                     // halves
     const size_t o = (size_t)mat * sT + (size_t)b * BT_NB * BT_NB;
     for (int j = 0; j < BT_NB; j++) {   // thread t writes Tt[j][t] = T[t][j]: row j, contiguous in t
         const float x = t <= j ? M[j * BT_LDM + t] : 0.f;
@@ -494,7 +540,7 @@ static cudaError_t backtransform_paired(const EighArgs &a, const SplitMat &Qs, c
         gx.push_back(g);
     }
     if ((e = multi_gemm(gx, nmat, s, nl)) != cudaSuccess) return e;
-    const size_t tsm = sizeof(float) * ((size_t)BT_NB * BT_LDM + BT_NB);
+    const size_t tsm = bt_tmat_smem();
     if ((e = cudaFuncSetAttribute(k_bt_tmat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm)) != cudaSuccess)
         return e;
     k_bt_tmat<<<dim3(nblk, nmat), BT_NB, tsm, s>>>(a, Gb, Tt, ms, ss);
@@ -619,7 +665,7 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
             const int np = min(CIR_SPLIT_MAXP, nblk - b0);
             if ((e = cir_launch_split_gemm_multi(gs.data() + b0, batch.data() + b0, np, s, &nl)) != cudaSuccess) return e;
         }
-        const size_t tsm = sizeof(float) * ((size_t)BT_NB * BT_LDM + BT_NB);
+        const size_t tsm = bt_tmat_smem();
         if ((e = cudaFuncSetAttribute(k_bt_tmat, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm)) != cudaSuccess)
             return e;
         k_bt_tmat<<<dim3(nblk, nmat), BT_NB, tsm, s>>>(a, Gb, Tt, ms, ss);
