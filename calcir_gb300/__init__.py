@@ -197,6 +197,18 @@ class Engine:
         V = np.ascontiguousarray(np.swapaxes(A, 1, 2))
         return (w[0], V[0]) if single else (w, V)
 
+    def tridiag_sbr(self, A):
+        """Two-stage reduction to tridiagonal form: (d, e, ms) with d, e [nmat][n] and the
+        device times of the two stages (dense -> band, band -> tridiagonal) in ms."""
+        A = np.ascontiguousarray(A, np.float32)
+        A = A.reshape(-1, A.shape[-1], A.shape[-1])
+        n = A.shape[-1]
+        d = np.empty((A.shape[0], n), np.float32)
+        e = np.empty((A.shape[0], n), np.float32)
+        ms = np.zeros(2, np.float32)
+        check(self.lib.cir_tridiag_sbr(self.h, A.shape[0], n, ptr(A), ptr(d), ptr(e), ptr(ms)))
+        return d, e, ms
+
     def propagate(self, V, w, dt, F):
         """F <- V diag(exp(i w dt/hbar)) V^T F; V holds eigenvectors as columns."""
         V = np.asarray(V, np.float32)

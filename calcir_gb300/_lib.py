@@ -108,6 +108,7 @@ SIGNATURES = {
     "cir_build_hamiltonian": [P, C.c_int, P, P, P, P, P, P],
     "cir_eigh": [P, C.c_int, C.c_int, P, P],
     "cir_eigh_noalloc": [C.c_int, C.c_int, P, P, P],
+    "cir_tridiag_sbr": [P, C.c_int, C.c_int, P, P, P, P],
     "cir_propagate": [P, C.c_int, C.c_int, P, P, C.c_float, P],
     "cir_tcf_terms": [P, C.c_int, P, P, P, P, P, P],
     "cir_spectral_density": [P, C.c_int, P, P, P, P],

@@ -423,6 +423,30 @@ extern "C" int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w) {
     return CIR_OK;
 }
 
+extern "C" int cir_tridiag_sbr(cir_ctx *c, int nmat, int n, const float *A, float *d, float *e, float *ms) {
+    if (!c || !A || !d || !e || nmat < 1 || n < 3) return cir_fail(CIR_ERR_ARG, "cir_tridiag_sbr: bad argument");
+    if (n > cir_sbr_max_n())
+        return cir_fail(CIR_ERR_ARG, "cir_tridiag_sbr: n = %d exceeds %d", n, cir_sbr_max_n());
+    if (nmat > 65535) return cir_fail(CIR_ERR_ARG, "cir_tridiag_sbr: %d matrices in one call (at most 65535)", nmat);
+    if (!is_device_ptr(A) && !all_finite(A, (size_t)nmat * n * n))
+        return cir_fail(CIR_ERR_NONFINITE, "cir_tridiag_sbr: the matrices contain NaN or Inf");
+    const int ld = (n + 7) & ~7;   // the pairs' rows start on 16-byte boundaries
+    CK(c->buf[B_PAD].ensure((size_t)nmat * n * ld * 4));
+    CK(c->buf[B_Z].ensure((size_t)nmat * cir_sbr_bytes(n, ld)));
+    CK(c->buf[B_IN1].ensure((size_t)nmat * n * 8));
+    CK(cudaMemcpy2DAsync(c->buf[B_PAD].p, (size_t)ld * 4, A, (size_t)n * 4, (size_t)n * 4, (size_t)nmat * n,
+                         cudaMemcpyDefault, c->stream));
+    float *dd = c->buf[B_IN1].as<float>(), *ee = dd + (size_t)nmat * n;
+    int launches = 0;
+    CK(cir_launch_sbr(c->buf[B_PAD].as<float>(), (long long)n * ld, nmat, n, ld, dd, ee, c->buf[B_Z].p,
+                      c->buf[B_ERR].as<int>(), c->stream, ms, &launches));
+    count_launch(c, launches);
+    CK(cudaMemcpyAsync(d, dd, (size_t)nmat * n * 4, cudaMemcpyDefault, c->stream));
+    CK(cudaMemcpyAsync(e, ee, (size_t)nmat * n * 4, cudaMemcpyDefault, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return check_kernel_flag(c);
+}
+
 // The optional FP64 refinement of the eigenpairs (refine_eigen steps): a copy of the nmat
 // input matrices at e.A, taken before the eigensolver overwrites them, and the workspace for
 // as many matrices at a time as fit in 2 GiB.

@@ -231,6 +231,13 @@ cudaError_t cir_launch_split_v(const float *A, int ld, long long sA, int n, Spli
 // Ft = I for the transposed complex F (real column c = 2q + {0: re, 1: im} at Ft[c*ldh ..])
 cudaError_t cir_launch_identity_t(SplitMat F, int n, int ldh, long long sF, int batch, cudaStream_t s, int *launches);
 
+// ---- two-stage reduction to tridiagonal form (k_sbr.cu): dense -> band on the split-BF16
+// tcgen05 GEMM, band -> tridiagonal by bulge chasing; d and e only (no eigenvectors) ----
+int cir_sbr_max_n();
+size_t cir_sbr_bytes(int n, int ld);   // work area per matrix (ld a multiple of 8)
+cudaError_t cir_launch_sbr(const float *H, long long sH, int nmat, int n, int ld, float *d, float *e, void *work,
+                           int *err, cudaStream_t s, float *ms, int *launches);
+
 // TCF terms: out[b][6] += (IR, VV, VH) for batch element b
 struct TcfArgs {
     const float *F;        // [batch] complex row-major, row stride ldf floats (2 per element)

@@ -7,6 +7,7 @@ CIR_EIGH_PROFILE=1 for the eigensolver's per-phase timers).
     python -m calcir_gb300.profile run --nmol 512 --nsamples 10 --ntcf 50 --propagate-vectors 1
     python -m calcir_gb300.profile grad --nmol 256 --nsamples 2 --ntcf 32
     python -m calcir_gb300.profile noalloc --nmol 256 --batch 16
+    python -m calcir_gb300.profile sbr --nmol 512 --batch 2500
 
 Every stage goes through the C ABI (libcalcir.so)."""
 from __future__ import annotations
@@ -52,6 +53,20 @@ def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32", **options)
     with cg.Engine(p, xyz.shape[1]) as eng:
         out = eng.run(xyz, box, fos)
         print(f"run nmol {nmol}: {out['frame_steps_per_s']:.1f} frame-steps/s", eng.stats(), flush=True)
+
+
+def sbr(nmol: int, nb: int, reps: int = 3) -> None:
+    """The two-stage reduction to tridiagonal form (cir_tridiag_sbr) on nb water Hamiltonians
+    (8 distinct frames repeated): the device times of its two stages."""
+    xyz, box = cg.synth_trajectory(nmol, 8, seed=3)
+    p = cg.default_params(model="tip4p2005", species="H2O", avef=3415.0)
+    with cg.Engine(p, xyz.shape[1]) as eng:
+        H, _, _, _ = eng.build_hamiltonian(xyz, box)
+        A = np.ascontiguousarray(np.broadcast_to(H[np.arange(nb) % 8], (nb,) + H.shape[1:]))
+        for r in range(reps):
+            d, e, ms = eng.tridiag_sbr(A)
+            print(f"sbr N={H.shape[-1]} batch {nb}: dense -> band {ms[0]:.1f} ms, band -> tridiagonal {ms[1]:.1f} ms",
+                  flush=True)
 
 
 def noalloc(nmol: int, nb: int) -> None:
@@ -105,6 +120,10 @@ def main() -> None:
     na = sub.add_parser("noalloc")
     na.add_argument("--nmol", type=int, default=256)
     na.add_argument("--batch", type=int, default=16)
+    sb = sub.add_parser("sbr")
+    sb.add_argument("--nmol", type=int, default=512)
+    sb.add_argument("--batch", type=int, default=2500)
+    sb.add_argument("--reps", type=int, default=3)
     gr = sub.add_parser("grad")
     gr.add_argument("--nmol", type=int, default=256)
     gr.add_argument("--nsamples", type=int, default=2)
@@ -116,6 +135,8 @@ def main() -> None:
         prop(a.n, a.nprop, a.precision)
     elif a.cmd == "grad":
         grad(a.nmol, a.nsamples, a.ntcf)
+    elif a.cmd == "sbr":
+        sbr(a.nmol, a.batch, a.reps)
     elif a.cmd == "noalloc":
         noalloc(a.nmol, a.batch)
     else:

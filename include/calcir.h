@@ -224,6 +224,16 @@ int cir_eigh(cir_ctx *c, int nmat, int n, float *A, float *w);
  * cudaMemcpyAsync into a host stack buffer and returns after cudaStreamSynchronize. */
 int cir_eigh_noalloc(int nmat, int n, float *A, float *w, void *cuda_stream);
 
+/* The two-stage reduction of nmat symmetric matrices A [nmat][n][n] to tridiagonal form
+ * (no counterpart in the reference, whose magma_ssyevd_gpu reduces in one stage,
+ * calcIR.cu:443-445): dense -> band of width 32 with the two-sided updates on the
+ * split-BF16 tensor-core GEMM, then band -> tridiagonal by bulge chasing.  d [nmat][n]
+ * receives the diagonal, e [nmat][n] the subdiagonal (e[n-1] = 0); their eigenvalues are
+ * A's to the split-BF16 precision (about 2^-16 of the spread of A's spectrum).  No
+ * eigenvectors: the reflectors of both stages are not kept.  n from 3 to 1025.  ms, when
+ * not NULL, receives the device time of the two stages in milliseconds. */
+int cir_tridiag_sbr(cir_ctx *c, int nmat, int n, const float *A, float *d, float *e, float *ms);
+
 /* One propagation step of nprop independent chains: F <- V diag(exp(+i w dt/hbar)) V^T F,
  * V [nprop][n][n] eigenvectors as returned by cir_eigh, w [nprop][n], F [nprop][n][n]
  * complex.  Replaces Pinit + 3 x magma_cgemm + magma_ccopy (calcIR.cu:596-617). */
