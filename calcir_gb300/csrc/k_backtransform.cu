@@ -282,6 +282,20 @@ __global__ void __launch_bounds__(256) k_bt_split_q(const float *Q, long long sQ
 // One thread block per reflector block and matrix: rows kb.. in chunks of BT_RC staged
 // like k_bt_prep's, written as pairs column-wise and, transposed through shared memory,
 // row-wise (columns j >= nbb of the row layout are zero).
+// eight values as BF16 hi and lo words at 16-byte aligned hi and lo
+__device__ __forceinline__ void store_pair8(__nv_bfloat16 *hi, __nv_bfloat16 *lo, const float (&x)[8]) {
+    uint32_t h[4], l[4];
+    #pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+        const __nv_bfloat162 hh = __floats2bfloat162_rn(x[e], x[e + 1]);
+        const __nv_bfloat162 ll = __floats2bfloat162_rn(x[e] - __bfloat162float(hh.x), x[e + 1] - __bfloat162float(hh.y));
+        h[e / 2] = *reinterpret_cast<const uint32_t *>(&hh);
+        l[e / 2] = *reinterpret_cast<const uint32_t *>(&ll);
+    }
+    *reinterpret_cast<uint4 *>(hi) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(lo) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
 // PAIRED: the row layout in the paired form (bt_yoff2), and both layouts from the pair's first
 // row, so that the second block's columns hold zeros above its reflectors.
 template <bool PAIRED>
@@ -300,14 +314,17 @@ __global__ void __launch_bounds__(BT_NT) k_bt_clean(EighArgs a, BtSplit sp) {
         __syncthreads();
         bt_stage(A, ld, n, kb, nbb, r0, false, Vt);
         __syncthreads();
-        for (int idx = t; idx < BT_NB * BT_RC; idx += BT_NT) {   // column layout, rows contiguous
-            const int j = idx / BT_RC, rr = idx - j * BT_RC, r = r0 + rr;
+        // the column layout 8 rows a thread, stored as 16-byte hi and lo words (ld is a multiple
+        // of 8 and the rows start on 8-row boundaries; rows past n, zero in Vt, fall in the
+        // column's padding below n)
+        for (int idx = t; idx < BT_NB * (BT_RC / 8); idx += BT_NT) {   // column layout, rows contiguous
+            const int j = idx / (BT_RC / 8), rr = 8 * (idx - j * (BT_RC / 8)), r = r0 + rr;
             if (j < nbb && r < n) {
-                const float x = Vt[j * BT_LDV + rr];
-                const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                const float4 x0 = *reinterpret_cast<const float4 *>(Vt + j * BT_LDV + rr);
+                const float4 x1 = *reinterpret_cast<const float4 *>(Vt + j * BT_LDV + rr + 4);
+                const float x[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
                 const size_t o = ov + (size_t)(kb + j) * sp.ldq + r;
-                sp.V.hi[o] = h;
-                sp.V.lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+                store_pair8(sp.V.hi + o, sp.V.lo + o, x);
             }
         }
         for (int idx = t; idx < BT_RC * wy; idx += BT_NT) {  // row layout, reflectors contiguous
