@@ -187,19 +187,29 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
     const uint32_t tmem = *tslot;
     constexpr uint32_t IDESC = make_idesc(C_::FMT);
 
-    Slice<!ACOL> la;    // A: K contiguous unless column-major
-    Slice<BKC> lb;      // B: N contiguous unless K-major
+    // two K slices in flight in registers: slice kt + 2 is requested right after slice kt is
+    // stored, so a load has two slices' MMA and staging time to arrive
+    Slice<!ACOL> la0, la1;   // A: K contiguous unless column-major
+    Slice<BKC> lb0, lb1;     // B: N contiguous unless K-major
     const int KT = (g.K + TK - 1) / TK;
     bool ok = true;
-    la.load(g.A + (size_t)bz * g.sA, g.lda, g.M, g.K, m0, 0);
-    lb.load(B, g.ldb, g.N, g.K, n0, 0);
-    for (int kt = 0; kt < KT; kt++) {
+    la0.load(A, g.lda, g.M, g.K, m0, 0);
+    lb0.load(B, g.ldb, g.N, g.K, n0, 0);
+    if (KT > 1) {
+        la1.load(A, g.lda, g.M, g.K, m0, TK);
+        lb1.load(B, g.ldb, g.N, g.K, n0, TK);
+    }
+    auto step = [&](int kt, Slice<!ACOL> &la, Slice<BKC> &lb) {
         const int s = kt & 1;
         if (kt >= 2) ok = mbar_wait(&bar[s], ((kt >> 1) - 1) & 1) && ok;   // MMAs that read stage s are done
         unsigned char *const pa[2] = {smem + s * STAGE, smem + s * STAGE + (C_::PARTS - 1) * TB};
         unsigned char *const pb[2] = {smem + s * STAGE + C_::PARTS * TB, smem + s * STAGE + (2 * C_::PARTS - 1) * TB};
         la.template store<MODE>(pa);
         lb.template store<MODE>(pb);
+        if (kt + 2 < KT) {
+            la.load(A, g.lda, g.M, g.K, m0, (kt + 2) * TK);
+            lb.load(B, g.ldb, g.N, g.K, n0, (kt + 2) * TK);
+        }
         fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
@@ -219,10 +229,10 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
             }
             mma_commit(&bar[s]);
         }
-        if (kt + 1 < KT) {
-            la.load(A, g.lda, g.M, g.K, m0, (kt + 1) * TK);
-            lb.load(B, g.ldb, g.N, g.K, n0, (kt + 1) * TK);
-        }
+    };
+    for (int kt = 0; kt < KT; kt += 2) {
+        step(kt, la0, lb0);
+        if (kt + 1 < KT) step(kt + 1, la1, lb1);
     }
     {   // the last commit covers every MMA issued before it
         const int last = KT - 1;
