@@ -534,18 +534,23 @@ __global__ void __launch_bounds__(PT, 1) k_tc_persist(const __grid_constant__ Pe
                 dd[3] = *reinterpret_cast<const uint4 *>(dl + 8);
                 return true;
             };
-            // two chunks in flight: the loads of chunk c0 + 32 are issued while c0 is processed
-            uint4 dnext[4], dnext2[4];
+            // three chunks in flight: the loads of chunk c0 + 48 are issued while c0 is processed
+            uint4 dnext[4], dnext2[4], dnext3[4];
             bool dnext_ok = dpre && dload(cbeg, dnext);
             bool dnext2_ok = dpre && cbeg + 16 < cend && dload(cbeg + 16, dnext2);
+            bool dnext3_ok = dpre && cbeg + 32 < cend && dload(cbeg + 32, dnext3);
             #pragma unroll 1
             for (int c0 = cbeg; c0 < cend; c0 += 16) {
                 uint4 dcur[4] = {dnext[0], dnext[1], dnext[2], dnext[3]};
                 const bool dcur_ok = dnext_ok;
                 #pragma unroll
-                for (int q = 0; q < 4; q++) dnext[q] = dnext2[q];
+                for (int q = 0; q < 4; q++) {
+                    dnext[q] = dnext2[q];
+                    dnext2[q] = dnext3[q];
+                }
                 dnext_ok = dnext2_ok;
-                if (dpre && c0 + 32 < cend) dnext2_ok = dload(c0 + 32, dnext2);
+                dnext2_ok = dnext3_ok;
+                if (dpre && c0 + 48 < cend) dnext3_ok = dload(c0 + 48, dnext3);
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * QN + c0), v);
                 if (r >= g.M) continue;
