@@ -59,6 +59,7 @@ enum {
     B_VS, B_FS,                                    // split-BF16 propagation operands
     B_UFR,                                         // run: distinct frames of a chunk and their multiplicity
     B_HREF, B_RW,                                  // FP64 eigenpair refinement: input copy, workspace
+    B_TQW,                                         // the panels' W of a joint tridiagonalisation
     B_COUNT
 };
 
@@ -903,11 +904,11 @@ struct GroupJob {
     // bytes of device memory one origin-step of a chunk holds from its preparation to the end
     // of its step loop (V, the eigenvalues, dipoles and polarisabilities, the status) ...
     static size_t resident_step_bytes(const cir_params &p, const Group &g) {
-        return (size_t)g.n * g.ld * 4 + (size_t)(9 + 1) * g.ld * 4 + 4;
+        return (size_t)g.n * g.ld * 4 + (size_t)(9 + 1) * g.ld * 4 + cir_eigh_de_bytes(g.ld) + 4;
     }
     // ... and during its preparation only (frames, tables, the eigensolver's work areas)
     static size_t scratch_step_bytes(const cir_params &p, const Group &g) {
-        return (size_t)(p.refine_eigen > 0 ? 2 : 1) * g.n * g.ld * 4 + cir_dc_bytes(g.n, g.ld) + cir_eigh_de_bytes(g.ld) +
+        return (size_t)(p.refine_eigen > 0 ? 2 : 1) * g.n * g.ld * 4 + cir_dc_bytes(g.n, g.ld) +
                (size_t)CT_NROW * g.ld * 4 + (size_t)g.natoms * 12 + 60;
     }
     static size_t per_step_bytes(const cir_params &p, const Group &g) {
@@ -945,7 +946,8 @@ struct GroupJob {
         CK(buf[B_A].ensure((size_t)nb * mstride * 4));
         CK(scr[B_Z].ensure((size_t)nb * mstride * 4));
         CK(scr[B_DC].ensure((size_t)nb * cir_dc_bytes(n, ld)));
-        CK(scr[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));
+        CK(buf[B_DE].ensure((size_t)nb * cir_eigh_de_bytes(ld)));   // d, e, tau: from the tridiagonalisation,
+                                                                   // which may run for several groups at once
         CK(buf[B_W].ensure((size_t)nb * ld * 4));
         CK(buf[B_M].ensure((size_t)nb * 9 * ld * 4));
         CK(buf[B_STATUS].ensure((size_t)nb * 4));
@@ -1037,6 +1039,27 @@ struct GroupJob {
     // Records ev[1] (start), ev[2] (built), ev[5] (tridiagonalised), ev[3] (done); with
     // account, waits for ev[3] and adds the build and eigensolver times to the stats.
     int prepare(int k0_, int kc_, bool account) {
+        int rc;
+        if ((rc = prepare_build(k0_, kc_, true))) return rc;
+        if ((rc = prepare_eig(false))) return rc;
+        if (account) {   // this group's build and eigensolve time, read now (the events are reused)
+            CK(cudaEventSynchronize(ev[3]));
+            float x;
+            cudaEventElapsedTime(&x, ev[1], ev[2]);
+            c->stats.ms_build += x;
+            cudaEventElapsedTime(&x, ev[2], ev[3]);
+            c->stats.ms_eig += x;
+            cudaEventElapsedTime(&x, ev[2], ev[5]);
+            c->stats.ms_tridiag += x;
+            if (p.verbose > 1) printf("  order %d, steps %d..%d: tridiagonalisation %.1f ms\n", n, k0, k0 + kc - 1, x);
+        }
+        return CIR_OK;
+    }
+
+    EighArgs eg{};   // the chunk's eigensolver arguments (prepare_build)
+
+    // gather and build the chunk's Hamiltonians and set up eg; events: record ev[1] and ev[2]
+    int prepare_build(int k0_, int kc_, bool events) {
         k0 = k0_;
         kc = kc_;
         int rc;
@@ -1075,7 +1098,7 @@ struct GroupJob {
                 CK(cudaMemcpyAsync(ufr + nmat, wgt.data(), (size_t)nmat * 4, cudaMemcpyHostToDevice, c->stream));
             }
         }
-        CK(cudaEventRecord(ev[1], c->stream));
+        if (events) CK(cudaEventRecord(ev[1], c->stream));
         if (ufr)
             k_gather_frames<<<dim3(8, nmat), 256, 0, c->stream>>>(dxyz, dbox, ufr, g.natoms, 1, nmat, nmat, 0,
                                                                   scr[B_CXYZ].as<float>(), scr[B_CBOX].as<float>());
@@ -1096,14 +1119,14 @@ struct GroupJob {
         a.dip_fstride = 9LL * ld;
         a.pol_fstride = 9LL * ld;
         CK(cir_launch_build(a, nmat, c->stream, &launches));
-        CK(cudaEventRecord(ev[2], c->stream));
-        EighArgs e;
+        if (events) CK(cudaEventRecord(ev[2], c->stream));
+        EighArgs &e = eg;
         memset(&e, 0, sizeof e);
         e.A = A;
         e.W = W;
         e.Z = scr[B_Z].as<float>();
         e.DC = scr[B_DC].as<float>();
-        e.DE = scr[B_DE].as<float>();
+        e.DE = buf[B_DE].as<float>();
         e.mstride = mstride;
         e.wstride = ld;
         e.n = n;
@@ -1136,6 +1159,14 @@ struct GroupJob {
         if (k0 == 0 && (rc = autotune_tridiag(c, e, nmat))) return rc;
         if (c->tq_blocks.count(n)) e.tq_blocks = c->tq_blocks[n];
         if ((rc = setup_refine(c, e, nmat))) return rc;
+        return CIR_OK;
+    }
+
+    // the eigensolver on eg (skip_tq: its tridiagonalisation has run already) and the step-0
+    // work; records ev[3] after the eigensolver
+    int prepare_eig(bool skip_tq) {
+        EighArgs &e = eg;
+        e.skip_tridiag = skip_tq ? 1 : 0;
         CK(cir_launch_eigh(e, nmat, c->stream, &launches));
         c->stats.eig_matrices += nmat;
         if (e.phase_ns) eigh_profile_report(e.phase_ns, nmat, c->stream);
@@ -1159,17 +1190,6 @@ struct GroupJob {
                 CK(cudaGetLastError());
             }
             launches++;
-        }
-        if (account) {   // this group's build and eigensolve time, read now (the events are reused)
-            CK(cudaEventSynchronize(ev[3]));
-            float x;
-            cudaEventElapsedTime(&x, ev[1], ev[2]);
-            c->stats.ms_build += x;
-            cudaEventElapsedTime(&x, ev[2], ev[3]);
-            c->stats.ms_eig += x;
-            cudaEventElapsedTime(&x, ev[2], ev[5]);
-            c->stats.ms_tridiag += x;
-            if (p.verbose > 1) printf("  order %d, steps %d..%d: tridiagonalisation %.1f ms\n", n, k0, k0 + kc - 1, x);
         }
         return CIR_OK;
     }
@@ -1430,6 +1450,81 @@ static bool joint_enabled() {
     return on;
 }
 
+// CIR_JOINT_TQ=0: in joint runs every group tridiagonalises its own chunks (for comparison)
+static bool joint_tq_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_JOINT_TQ");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+// The preparations of the groups whose chunks start at step k0.  When two or more of them
+// have orders 257-1024 (the blocked tridiagonalisation), their Hamiltonians are built one
+// group after another and tridiagonalised in one launch (cir_launch_tridiag_multi: the
+// longest matrices first, the shorter ones filling the last wave, each group's panel W in
+// one shared area), then each group's eigensolver goes on from its d, e and reflectors;
+// otherwise group by group.  The build time counted includes the autotuner's trials of the
+// first chunk.
+static int prepare_segment(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &jobs, const std::vector<int> &prep,
+                           int k0) {
+    const int K = c->p.ntcfpoints;
+    int rc;
+    std::vector<int> jt;
+    // (not with the eigenpair refinement, whose copy of the input matrices is one shared area)
+    if (joint_tq_enabled() && !eigh_profiling() && c->p.refine_eigen <= 0)
+        for (int i : prep)
+            if (jobs[i]->n > 256 && jobs[i]->n <= 1024) jt.push_back(i);
+    if (jt.size() < 2) {
+        for (int i : prep) {
+            GroupJob &j = *jobs[i];
+            if ((rc = j.prepare(k0, std::min(j.kn, K - k0), true))) return rc;
+        }
+        return CIR_OK;
+    }
+    cudaEvent_t *ev = c->ev;
+    CK(cudaEventRecord(ev[1], c->stream));
+    for (int i : prep) {
+        GroupJob &j = *jobs[i];
+        if ((rc = j.prepare_build(k0, std::min(j.kn, K - k0), false))) return rc;
+        j.eg.tq_done = nullptr;
+    }
+    CK(cudaEventRecord(ev[2], c->stream));
+    size_t wf = 0;
+    for (int i : jt) wf += (size_t)jobs[i]->nmat * cir_tridiag_w_floats(jobs[i]->ld);
+    CK(c->buf[B_TQW].ensure(wf * 4));
+    EighArgs a[CIR_TQ_MAXP];
+    int nm[CIR_TQ_MAXP];
+    size_t off = 0;
+    for (size_t q = 0; q < jt.size(); q++) {
+        GroupJob &j = *jobs[jt[q]];
+        a[q] = j.eg;
+        a[q].Z = c->buf[B_TQW].as<float>() + off;
+        a[q].zstride = (long long)cir_tridiag_w_floats(j.ld);
+        nm[q] = j.nmat;
+        off += (size_t)j.nmat * a[q].zstride;
+    }
+    CK(cir_launch_tridiag_multi(a, nm, (int)jt.size(), c->stream, &jobs[jt[0]]->launches));
+    CK(cudaEventRecord(ev[5], c->stream));
+    for (int i : prep)
+        if ((rc = jobs[i]->prepare_eig(std::find(jt.begin(), jt.end(), i) != jt.end()))) return rc;
+    CK(cudaEventRecord(ev[3], c->stream));
+    CK(cudaEventSynchronize(ev[3]));
+    float x;
+    cudaEventElapsedTime(&x, ev[1], ev[2]);
+    c->stats.ms_build += x;
+    cudaEventElapsedTime(&x, ev[2], ev[3]);
+    c->stats.ms_eig += x;
+    cudaEventElapsedTime(&x, ev[2], ev[5]);
+    c->stats.ms_tridiag += x;
+    if (c->p.verbose > 1) {
+        printf("  steps %d..: one tridiagonalisation launch for orders", k0);
+        for (int i : jt) printf(" %d (%d matrices)", jobs[i]->n, jobs[i]->nmat);
+        printf(": %.1f ms\n", x);
+    }
+    return CIR_OK;
+}
+
 // Up to CIR_SPLIT_MAXP size groups of one cir_run_multi job in the split-BF16 form, run in
 // lockstep: per chunk every group's frames are built and diagonalised with its own buffers,
 // then each step of the chunk is one persistent launch of G = V^T F over the origins of all
@@ -1488,12 +1583,11 @@ static int run_groups_joint(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &
     std::vector<int> next(ng, 0);   // first step not covered by each group's prepared chunk
     CK(cudaEventRecord(ev[0], c->stream));
     for (int k0 = 0; k0 < K;) {
+        std::vector<int> prep;
         for (int i = 0; i < ng; i++)
-            if (next[i] == k0) {
-                GroupJob &j = *jobs[i];
-                if ((rc = j.prepare(k0, std::min(j.kn, K - k0), true))) return rc;
-                next[i] = k0 + j.kc;
-            }
+            if (next[i] == k0) prep.push_back(i);
+        if ((rc = prepare_segment(c, jobs, prep, k0))) return rc;
+        for (int i : prep) next[i] = k0 + jobs[i]->kc;
         const int k1 = *std::min_element(next.begin(), next.end());   // steps k0 .. k1 - 1 run jointly
         CK(cudaEventRecord(ev[3], c->stream));
         std::vector<long long> key = {-1, ng, k0, k1};

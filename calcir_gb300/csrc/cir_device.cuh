@@ -124,6 +124,12 @@ struct EighArgs {
     // thread blocks of the tridiagonalisation per SM: 0 the kernel's own occupancy, or a
     // smaller count enforced through its shared-memory request (the autotuner's choice)
     int tq_blocks;
+    // per-matrix stride of Z in the tridiagonalisation (0: mstride), which keeps only the
+    // panel's W there (cir_tridiag_w_floats(ld) floats per matrix)
+    long long zstride;
+    // 1: cir_launch_eigh starts after the tridiagonalisation (d, e, tau already in DE and the
+    // reflectors in A, as cir_launch_tridiag_multi leaves them)
+    int skip_tridiag;
 };
 
 // kernel launchers (return cudaError_t of the launch)
@@ -133,6 +139,12 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
 cudaError_t cir_launch_tridiag(const EighArgs &a, int nmat, cudaStream_t s);
 // thread blocks per SM the tridiagonalisation of order n runs with by default
 int cir_tridiag_blocks(int n);
+// The tridiagonalisations of up to CIR_TQ_MAXP batches of orders 257-1024 (boxes of different
+// size) in one launch, the longest matrices first; a[i] as for cir_launch_tridiag (tq_blocks
+// is not applied: the kernel's own occupancy).
+constexpr int CIR_TQ_MAXP = 4;
+cudaError_t cir_launch_tridiag_multi(const EighArgs *a, const int *nmat, int np, cudaStream_t s, int *launches);
+size_t cir_tridiag_w_floats(int ld);   // the tridiagonalisation's use of Z per matrix
 size_t cir_eigh_rot_bytes(int n);
 size_t cir_eigh_de_bytes(int ld);
 size_t cir_dc_bytes(int n, int ld);

@@ -708,15 +708,16 @@ __device__ void tridiag_blocked(float *__restrict__ A, float *__restrict__ Wb, i
     __syncthreads();
 }
 
-template <int NT, int NMAX, int MINB, bool BLK>
-__global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
+// Phase 1 of matrix `mat` of a (the body of k_eigh_tq and of k_eigh_tq_multi).
+template <int NT, int NMAX, bool BLK>
+__device__ __forceinline__ void tq_body(const EighArgs &a, int mat) {
     constexpr int QG = (NMAX + 4 * NT - 1) / (4 * NT); // 4-row groups per thread, phase 1
     constexpr int NW = NT / 32;
     extern __shared__ __align__(16) float smem[];
     const int n = a.n, ld = a.ld;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    float *A = a.A + (size_t)blockIdx.x * a.mstride;
-    float *Z = a.Z + (size_t)blockIdx.x * a.mstride;
+    float *A = a.A + (size_t)mat * a.mstride;
+    float *Z = a.Z + (size_t)mat * (a.zstride ? a.zstride : a.mstride);
 
     const int n4 = (n + 3) & ~3;
     float *d = smem;             // [n4]
@@ -725,9 +726,9 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     float *U = tau + n4;         // union region (tq_union_floats)
     float *red = U + tq_union_floats(n, NT, BLK);   // [64]
 
-    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)blockIdx.x * CIR_EIG_PROF_SLOTS : nullptr;
+    unsigned long long *pt = a.phase_ns ? a.phase_ns + (size_t)mat * CIR_EIG_PROF_SLOTS : nullptr;
     if (pt && tid == 0) pt[0] = globaltimer_ns();
-    if (a.status && tid == 0) a.status[blockIdx.x] = 0;
+    if (a.status && tid == 0) a.status[mat] = 0;
     // ---------------- phase 1: tridiagonalisation ----------------
     if constexpr (BLK) {
         // W of the current panel lives in Z, which phase 2 overwrites
@@ -886,7 +887,7 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
     }
 
     // d, e and tau for the next two kernels
-    float *de = a.DE + (size_t)blockIdx.x * 3 * ld;
+    float *de = a.DE + (size_t)mat * 3 * ld;
     for (int i = tid; i < n; i += NT) {
         de[i] = d[i];
         de[ld + i] = e[i];
@@ -896,6 +897,28 @@ __global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
         __syncthreads();
         if (tid == 0) pt[1] = globaltimer_ns();
     }
+}
+
+template <int NT, int NMAX, int MINB, bool BLK>
+__global__ void __launch_bounds__(NT, MINB) k_eigh_tq(EighArgs a) {
+    tq_body<NT, NMAX, BLK>(a, blockIdx.x);
+}
+
+// Several batches of the blocked form in one launch (orders 257-1024, the order-1024
+// instantiation for all): problem p covers blocks start[p] .. start[p+1]-1, the problems in
+// descending order, so that the longest matrices start first and the shorter ones fill
+// the last wave.
+struct TqPlan {
+    EighArgs a[CIR_TQ_MAXP];
+    int start[CIR_TQ_MAXP + 1];
+    int np;
+};
+
+template <int NT, int NMAX, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_eigh_tq_multi(const __grid_constant__ TqPlan plan) {
+    int p = 0;
+    while (p + 1 < plan.np && (int)blockIdx.x >= plan.start[p + 1]) p++;
+    tq_body<NT, NMAX, true>(plan.a[p], (int)blockIdx.x - plan.start[p]);
 }
 
 // Sum NV per-lane values over the warp by halving exchanges (lane bit 4 first): lane L ends
@@ -1328,6 +1351,45 @@ int cir_eigh_max_n() { return 2048; }
 
 int cir_tridiag_blocks(int n) { return n <= 256 ? 4 : (n <= 1024 ? 3 : 2); }
 
+size_t cir_tridiag_w_floats(int ld) { return (size_t)TB_NB * ld; }
+
+cudaError_t cir_launch_tridiag_multi(const EighArgs *a, const int *nmat, int np, cudaStream_t s, int *launches) {
+    if (np < 1 || np > CIR_TQ_MAXP) return cudaErrorInvalidValue;
+    int order[CIR_TQ_MAXP];
+    for (int i = 0; i < np; i++) {
+        const EighArgs &x = a[i];
+        if (x.n <= 256 || x.n > 1024 || nmat[i] < 1 || nmat[i] > 65535 || (x.ld & 3) || x.ld < x.n || !x.DE ||
+            (reinterpret_cast<uintptr_t>(x.A) & 15) || (reinterpret_cast<uintptr_t>(x.Z) & 15))
+            return cudaErrorInvalidValue;
+        order[i] = i;
+    }
+    std::sort(order, order + np, [&](int x, int y) { return a[x].n > a[y].n; });
+    static const int tq_order = [] {
+        const char *v = getenv("CIR_TQ_ORDER");
+        return v ? atoi(v) : 1;
+    }();
+    TqPlan plan;
+    memset(&plan, 0, sizeof plan);
+    plan.np = np;
+    size_t smem = 0;
+    int total = 0;
+    for (int k = 0; k < np; k++) {
+        plan.a[k] = a[order[k]];
+        plan.a[k].tq_order = tq_order;
+        plan.start[k] = total;
+        total += nmat[order[k]];
+        smem = std::max(smem, tq_smem_bytes(plan.a[k].n, 256, true));
+    }
+    plan.start[np] = total;
+    auto kern = k_eigh_tq_multi<256, 1024, 3>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<total, 256, smem, s>>>(plan);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (launches) *launches += 1;
+    return cudaSuccess;
+}
+
 cudaError_t cir_launch_tridiag(const EighArgs &a, int nmat, cudaStream_t s) {
     if (a.n <= 256) return launch_tq<128, 256, 4, false>(a, nmat, s);
     if (a.n <= 512) return launch_tq<256, 512, 3, true>(a, nmat, s);
@@ -1341,10 +1403,12 @@ cudaError_t cir_launch_eigh(const EighArgs &a, int nmat, cudaStream_t s, int *la
     if ((reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15) || !a.DE ||
         (!a.rot && !a.DC) || (a.DC && (reinterpret_cast<uintptr_t>(a.DC) & 15)))
         return cudaErrorInvalidValue;
-    cudaError_t e = cir_launch_tridiag(a, nmat, s);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
+    if (!a.skip_tridiag) {
+        if ((e = cir_launch_tridiag(a, nmat, s)) != cudaSuccess) return e;
+        if (launches) *launches += 1;
+    }
     if (a.tq_done && (e = cudaEventRecord(a.tq_done, s)) != cudaSuccess) return e;
-    if (launches) *launches += 1;
     // divide and conquer: the reflectors are applied to the tridiagonal eigenvectors at the end
     if (a.DC) return cir_launch_dc(a, nmat, s, launches);
     if (a.n <= 512) e = launch_formq<256, 512, 16, 8, 2>(a, nmat, s);

@@ -182,3 +182,19 @@ def test_run_multi_joint_split_launches_match_single_runs(lib):
         _same(multi[i], single, 1e-5, f"trajectory {i} ({sizes[i]} molecules), joint split-BF16")
     print("kernel launches: joint", joint_launches, "one size at a time", single_launches)
     assert joint_launches < single_launches
+
+
+def test_run_multi_joint_tridiagonalisation_matches_single_runs(lib):
+    """With two or more box sizes of orders 257-1024 starting a chunk together, the joint
+    split-BF16 run tridiagonalises all their Hamiltonians in one launch (the longest matrices
+    first) before each size's eigensolver goes on; each trajectory's results equal cir_run's
+    for it alone."""
+    prm, p = _params(lib, precision="bf16x3")
+    sizes = [144, 200, 144]            # orders 288 and 400
+    trajs = _trajectories(lib, prm, sizes)
+    with lib.Engine(p, sizes[0] * 4) as eng:
+        multi = eng.run_multi(trajs)
+    for i, (xyz, box, fos) in enumerate(trajs):
+        with lib.Engine(p, xyz.shape[1]) as eng:
+            single = eng.run(xyz, box, fos)
+        _same(multi[i], single, 1e-5, f"trajectory {i} ({sizes[i]} molecules), joint tridiagonalisation")
