@@ -8,6 +8,7 @@ CIR_EIGH_PROFILE=1 for the eigensolver's per-phase timers).
     python -m calcir_gb300.profile grad --nmol 256 --nsamples 2 --ntcf 32
     python -m calcir_gb300.profile noalloc --nmol 256 --batch 16
     python -m calcir_gb300.profile sbr --nmol 512 --batch 2500
+    python -m calcir_gb300.profile multi --sizes 128,216,343,512 --ntraj 4 --ntcf 200
 
 Every stage goes through the C ABI (libcalcir.so)."""
 from __future__ import annotations
@@ -53,6 +54,22 @@ def run(nmol: int, nsamples: int, ntcf: int, precision: str = "fp32", **options)
     with cg.Engine(p, xyz.shape[1]) as eng:
         out = eng.run(xyz, box, fos)
         print(f"run nmol {nmol}: {out['frame_steps_per_s']:.1f} frame-steps/s", eng.stats(), flush=True)
+
+
+def multi(sizes: list[int], ntraj: int, ntcf: int) -> None:
+    """One cir_run_multi job in the split-BF16 form over boxes of the given sizes (ntraj
+    trajectories each, one origin of ntcf points), the autotuner off: the joint
+    tridiagonalisation and propagation launches."""
+    trajs = []
+    for nmol in sizes:
+        for t in range(ntraj):
+            xyz, box = cg.synth_trajectory(nmol, ntcf, seed=1000 + 7 * nmol + t)
+            trajs.append((xyz, box, None))
+    p = cg.default_params(model="tip4p2005", species="H2O", ntcfpoints=ntcf, nsamples=1, sampleEvery=2.0,
+                          avef=3415.0, omegaStart=2000, omegaStop=5000, omegaStep=1, precision="bf16x3", autotune=0)
+    with cg.Engine(p, 4 * sizes[0]) as eng:
+        eng.run_multi(trajs)
+        print(f"multi {sizes} x {ntraj}:", eng.stats(), flush=True)
 
 
 def sbr(nmol: int, nb: int, reps: int = 3) -> None:
@@ -120,6 +137,10 @@ def main() -> None:
     na = sub.add_parser("noalloc")
     na.add_argument("--nmol", type=int, default=256)
     na.add_argument("--batch", type=int, default=16)
+    mu = sub.add_parser("multi")
+    mu.add_argument("--sizes", default="128,216,343,512")
+    mu.add_argument("--ntraj", type=int, default=4)
+    mu.add_argument("--ntcf", type=int, default=200)
     sb = sub.add_parser("sbr")
     sb.add_argument("--nmol", type=int, default=512)
     sb.add_argument("--batch", type=int, default=2500)
@@ -135,6 +156,8 @@ def main() -> None:
         prop(a.n, a.nprop, a.precision)
     elif a.cmd == "grad":
         grad(a.nmol, a.nsamples, a.ntcf)
+    elif a.cmd == "multi":
+        multi([int(x) for x in a.sizes.split(",")], a.ntraj, a.ntcf)
     elif a.cmd == "sbr":
         sbr(a.nmol, a.batch, a.reps)
     elif a.cmd == "noalloc":
