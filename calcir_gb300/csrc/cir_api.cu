@@ -79,6 +79,8 @@ struct cir_ctx {
     int natoms = 0, nmol = 0, n = 0, ld = 0;
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
+    cudaStream_t aux = nullptr;   // the second half of a split eigensolver batch
+    cudaEvent_t xev[3] = {};      // fork, its tridiagonalisation done, join
     DevBuf buf[B_COUNT];
     cir_stats stats;
     cudaEvent_t ev[8];
@@ -264,6 +266,9 @@ extern "C" int cir_destroy(cir_ctx *c) {
     for (auto &gb : c->gbuf)
         for (int i = 0; i < B_COUNT; i++) gb[i].release();
     for (auto &e : c->ev) cudaEventDestroy(e);
+    for (auto &e : c->xev)
+        if (e) cudaEventDestroy(e);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return CIR_OK;
@@ -830,6 +835,15 @@ static std::vector<long long> step_key(const Group &g, int St, int K, int k0, in
 static int psi_propagate(cir_ctx *c, int S, int n, int ld, const float *V, long long sV, const float *w, long long sw,
                          float dt, float *x, float *tmp, int &launches);
 
+// CIR_EIG_SPLIT=0: the eigensolver batch of a chunk in one stream, not two (for comparison)
+static bool eig_split_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_EIG_SPLIT");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 // Thread blocks of the tridiagonalisation of order n resident at a time (one per matrix).
 static int tridiag_wave(cir_ctx *c, int n) {
     int dev = 0, sms = 0;
@@ -1041,7 +1055,7 @@ struct GroupJob {
     int prepare(int k0_, int kc_, bool account) {
         int rc;
         if ((rc = prepare_build(k0_, kc_, true))) return rc;
-        if ((rc = prepare_eig(false))) return rc;
+        if ((rc = prepare_eig(false, true))) return rc;
         if (account) {   // this group's build and eigensolve time, read now (the events are reused)
             CK(cudaEventSynchronize(ev[3]));
             float x;
@@ -1049,7 +1063,7 @@ struct GroupJob {
             c->stats.ms_build += x;
             cudaEventElapsedTime(&x, ev[2], ev[3]);
             c->stats.ms_eig += x;
-            cudaEventElapsedTime(&x, ev[2], ev[5]);
+            x = tridiag_ms();
             c->stats.ms_tridiag += x;
             if (p.verbose > 1) printf("  order %d, steps %d..%d: tridiagonalisation %.1f ms\n", n, k0, k0 + kc - 1, x);
         }
@@ -1057,6 +1071,57 @@ struct GroupJob {
     }
 
     EighArgs eg{};   // the chunk's eigensolver arguments (prepare_build)
+
+    bool split_done = false;   // the last prepare_eig ran two parts (split_eig)
+
+    // ms from the end of the build (ev[2]) to the end of the tridiagonalisation: of the later
+    // part when the batch ran in two (the events are complete once ev[3] is)
+    float tridiag_ms() const {
+        float x = 0.f;
+        cudaEventElapsedTime(&x, ev[2], ev[5]);
+        if (split_done) {
+            float y = 0.f, z = 0.f;
+            cudaEventElapsedTime(&y, ev[2], c->xev[1]);
+            if (p.verbose > 1) {
+                cudaEventElapsedTime(&z, ev[2], ev[3]);
+                printf("  two parts: tridiagonalisations end at %.1f and %.1f ms, eigensolver at %.1f ms\n", x, y, z);
+            }
+            x = std::max(x, y);
+        }
+        return x;
+    }
+
+    // eg over matrices [0, hA) on the library stream and [hA, nmat) on c->aux, joined before
+    // the library stream goes on; the two tridiagonalisations end at ev[5] and c->xev[1]
+    int split_eig(int hA) {
+        if (!c->aux) {
+            int lo = 0, hi = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            CK(cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, lo));
+            for (auto &x : c->xev) CK(cudaEventCreate(&x));
+        }
+        const int hB = nmat - hA;
+        EighArgs a = eg, b = eg;
+        a.tq_done = ev[5];
+        b.tq_done = c->xev[1];
+        b.A = eg.A + (size_t)hA * mstride;
+        b.W = eg.W + (size_t)hA * eg.wstride;
+        b.Z = eg.Z + (size_t)hA * mstride;
+        b.DE = eg.DE + (size_t)hA * 3 * ld;
+        b.DC = eg.DC + (size_t)3 * hA * mstride;   // [3][hB] after the first part's [3][hA]
+        b.status = eg.status + hA;
+        if (eg.hist_weight) b.hist_weight = eg.hist_weight + hA;
+        if (eg.hist_group) b.hist_group = 0;
+        if (eg.hist_group) a.hist_group = 0;
+        CK(cudaEventRecord(c->xev[0], c->stream));
+        CK(cudaStreamWaitEvent(c->aux, c->xev[0], 0));
+        CK(cir_launch_eigh(a, hA, c->stream, &launches));
+        CK(cir_launch_eigh(b, hB, c->aux, &launches));
+        CK(cudaEventRecord(c->xev[2], c->aux));
+        CK(cudaStreamWaitEvent(c->stream, c->xev[2], 0));
+        split_done = true;
+        return CIR_OK;
+    }
 
     // gather and build the chunk's Hamiltonians and set up eg; events: record ev[1] and ev[2]
     int prepare_build(int k0_, int kc_, bool events) {
@@ -1164,10 +1229,25 @@ struct GroupJob {
 
     // the eigensolver on eg (skip_tq: its tridiagonalisation has run already) and the step-0
     // work; records ev[3] after the eigensolver
-    int prepare_eig(bool skip_tq) {
+    int prepare_eig(bool skip_tq, bool may_split = false) {
         EighArgs &e = eg;
         e.skip_tridiag = skip_tq ? 1 : 0;
-        CK(cir_launch_eigh(e, nmat, c->stream, &launches));
+        split_done = false;
+        int hA = 0;   // the first part: whole waves of the tridiagonalisation, all but the last one
+        if (may_split && !skip_tq && eig_split_enabled() && !e.Href && !e.phase_ns &&
+            (e.hist_group == 0 || e.hist_group >= nmat)) {
+            const int wave = tridiag_wave(c, n);
+            if (nmat >= 2 * wave) hA = (nmat / wave - 1) * wave;
+        }
+        if (hA > 0 && hA < nmat) {
+            // the batch in two parts on two streams: the first (whole waves) on the library
+            // stream, the rest on a second one, so that the first part's divide and conquer
+            // and back-transform can start while the rest is still being tridiagonalised
+            int rc;
+            if ((rc = split_eig(hA))) return rc;
+        } else {
+            CK(cir_launch_eigh(e, nmat, c->stream, &launches));
+        }
         c->stats.eig_matrices += nmat;
         if (e.phase_ns) eigh_profile_report(e.phase_ns, nmat, c->stream);
         CK(cudaEventRecord(ev[3], c->stream));
@@ -1426,7 +1506,7 @@ static int run_group(cir_ctx *c, const Group &g, const float *dxyz, const float 
         c->stats.ms_build += x;
         cudaEventElapsedTime(&x, ev[2], ev[3]);
         c->stats.ms_eig += x;
-        cudaEventElapsedTime(&x, ev[2], ev[5]);
+        x = j.tridiag_ms();
         c->stats.ms_tridiag += x;
         if (c->p.verbose > 1) printf("  order %d, steps %d..%d: tridiagonalisation %.1f ms\n", j.n, k0, k0 + j.kc - 1, x);
         cudaEventElapsedTime(&x, ev[3], ev[4]);
@@ -1507,7 +1587,7 @@ static int prepare_segment(cir_ctx *c, std::vector<std::unique_ptr<GroupJob>> &j
     CK(cir_launch_tridiag_multi(a, nm, (int)jt.size(), c->stream, &jobs[jt[0]]->launches));
     CK(cudaEventRecord(ev[5], c->stream));
     for (int i : prep)
-        if ((rc = jobs[i]->prepare_eig(std::find(jt.begin(), jt.end(), i) != jt.end()))) return rc;
+        if ((rc = jobs[i]->prepare_eig(std::find(jt.begin(), jt.end(), i) != jt.end(), false))) return rc;
     CK(cudaEventRecord(ev[3], c->stream));
     CK(cudaEventSynchronize(ev[3]));
     float x;
