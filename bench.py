@@ -152,20 +152,20 @@ PARITY_FIXTURE = os.path.join(ROOT, "tests", "golden", "fullsize_512h2o.npz")
 PARITY_KEYS = ("tcf_ir", "tcf_vv", "tcf_vh", "ls_ir", "ls_vv", "ls_vh", "sw")
 
 
-def parity(out, seed, bound):
+def parity(out, seed, bound, fixture=PARITY_FIXTURE):
     """Relative L2 error of each spectrum of a timed job against the FP64 oracle's spectra of
-    the same job (512 H2O, 10 origins x 250 points, frames of seed 1), stored as a fixture
-    by tests/golden/make_fullsize.py."""
-    if seed != 1 or not os.path.exists(PARITY_FIXTURE):
+    the same job (512 H2O, 10 origins x 250 points, frames of seed 1; or the fixture given),
+    stored as a fixture by tests/golden/make_fullsize.py."""
+    if seed != 1 or not os.path.exists(fixture):
         return {"note": "no oracle fixture for this seed"}
-    z = np.load(PARITY_FIXTURE)
+    z = np.load(fixture)
     errs = {}
     for k in PARITY_KEYS:
         a, b = np.asarray(out[k]), z["fin_" + k]
         if a.shape != b.shape:
             return {"note": f"{k}: shape {a.shape} != fixture {b.shape}"}
         errs[k] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    return {"vs": "FP64 oracle, the same job (tests/golden/fullsize_512h2o.npz)", "rel_l2": errs,
+    return {"vs": f"FP64 oracle, the same job (tests/golden/{os.path.basename(fixture)})", "rel_l2": errs,
             "bound": bound, "within_bound": all(v < bound for v in errs.values())}
 
 
@@ -298,6 +298,69 @@ DIFF_JOB = dict(model="tip4p2005", species="H2O", ntcfpoints=200, nsamples=4, sa
                 avef=3415.0, omegaStart=2000, omegaStop=5000, omegaStep=1, nzeros=25600, map=0)
 
 
+PRECISION_FIXTURE = os.path.join(ROOT, "tests", "golden", "fullsize_1024h2o.npz")
+
+
+def run_precision(args):
+    """The precision configuration: 1024 TIP4P/2005 molecules (2048 chromophores), 5 time
+    origins 2 ps apart x 250 points = 1250 frame-steps per job, on seeded frames (seed 1).
+    Each form -- the plain FP32 form and the mixed split-BF16 and TF32 forms -- is timed over
+    --steps jobs after --warmup jobs, and its spectra are compared with the FP64 oracle's of
+    the same job (bound 1e-4 for the plain form, 1e-3 for the mixed forms).  The line's value
+    is the split-BF16 form's (the refinement option, about 46 ms per order-2048 matrix and
+    step in FP64, is checked by the tests, not timed here)."""
+    import torch
+    torch.cuda.set_device(0)
+    from calcir_gb300 import build
+    build.build()
+    import calcir_gb300 as cg
+    job = dict(JOB, nsamples=5)
+    p = cg.default_params(**job)
+    fos = cg.frame_table(p, 0.010)
+    xyz, box = cg.synth_trajectory(1024, int(fos.max()) + 1, seed=1)
+    d_xyz = torch.from_numpy(xyz).cuda()
+    d_box = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(box, (xyz.shape[0], 3)))).cuda()
+    stream = torch.cuda.current_stream()
+    steps, warm = max(1, args.steps), max(1, min(args.warmup, 2))
+    forms = {}
+    sampler = ClockSampler(gpu_identifier())
+    for name, prec, bound in (("split-BF16", "bf16x3", 1e-3), ("TF32", "tf32", 1e-3), ("plain FP32", "fp32", 1e-4)):
+        q = cg.default_params(**job, precision=prec)
+        with cg.Engine(q, xyz.shape[1]) as eng:
+            eng.set_stream(stream.cuda_stream)
+            for _ in range(warm):
+                eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+            eng.reset_stats()
+            torch.cuda.synchronize()
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(steps):
+                out = eng.run(d_xyz.data_ptr(), d_box.data_ptr(), fos, nframes=xyz.shape[0])
+            t1.record(stream)
+            torch.cuda.synchronize()
+            ms = t0.elapsed_time(t1)
+            st = eng.stats()
+        forms[name] = {"value": len(fos) * steps / (ms * 1e-3), "unit": "frame-steps/s", "ms_per_step": ms / steps,
+                       "stages_ms_per_step": {k: st[k] / steps for k in ("ms_build", "ms_eig", "ms_prop")},
+                       "parity": parity(out, 1, bound, PRECISION_FIXTURE)}
+    clk = sampler.stop()
+    head = forms["split-BF16"]
+    line = {
+        "metric": "frame-steps/s, precision: 1024 H2O (2048 chromophores), 5 origins x 250 points",
+        "value": head["value"], "unit": "frame-steps/s", "n_gpus": 1, "steps": steps, "warmup": warm,
+        "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+bf16x3", "data": "synthetic",
+        "config": {"workload": "1024 TIP4P/2005 molecules (2048 chromophores), 5 time origins 2 ps apart x 250 "
+                               "correlation points at 10 fs = 1250 frame-steps per step", "seed": 1},
+        "forms": forms,
+        "mixed_over_plain": head["value"] / forms["plain FP32"]["value"],
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_differentiation(args):
     """The differentiation configuration: 256 TIP4P/2005 molecules (512 chromophores), 4 time
     origins x 200 points; the loss is the IR + VV lineshape mismatch against targets made by
@@ -377,9 +440,10 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=8, help="frame-steps per CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="full", choices=["full", "batching", "differentiation"],
+    ap.add_argument("--workload", default="full", choices=["full", "batching", "differentiation", "precision"],
                     help="full: the 512 H2O job (the headline); batching: uneven boxes of 128/216/343/512 "
-                         "molecules, --batching-traj trajectories of each size, in one cir_run_multi job")
+                         "molecules, --batching-traj trajectories of each size, in one cir_run_multi job; "
+                         "differentiation: loss + gradient at 256 H2O; precision: 1024 H2O, 5 x 250, each form")
     ap.add_argument("--batching-traj", type=int, default=32)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -388,6 +452,8 @@ def main():
         return run_batching(args)
     if args.workload == "differentiation":
         return run_differentiation(args)
+    if args.workload == "precision":
+        return run_precision(args)
 
     import torch
     rank, world, local = dist_env()
