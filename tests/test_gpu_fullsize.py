@@ -10,7 +10,8 @@ seeded frames and stored as a fixture (tests/golden/make_fullsize.py):
 Every form runs the same job through the C ABI (cir_run) and is held to the bound its form
 states, per spectrum (IR, VV, VH correlation functions and lineshapes, spectral density):
 the plain FP32 form within 1e-4 relative L2, the mixed forms (split-BF16 and TF32 tensor-core
-GEMMs, with and without the FP64 eigenpair refinement) within 1e-3.  The frequency
+GEMMs, with and without the FP64 eigenpair refinement, and the split-BF16 form with frame
+sharing or the psi-vector propagation) within 1e-3.  The frequency
 distributions agree up to bin flips of eigenvalues that sit on a bin edge.
 """
 import os
@@ -54,7 +55,10 @@ def _params(lib, prm, **extra):
     return lib.default_params(model="tip4p2005", species="H2O", **keys)
 
 
-FORMS = [("fp32", {}), ("bf16x3", {}), ("tf32", {}), ("bf16x3+refine2", {"refine_eigen": 2})]
+# the options of the same job (distinct frames diagonalised once; psi = F m(0) propagated)
+# run the split eigensolver's two streams with the frame weights and the vector propagation
+FORMS = [("fp32", {}), ("bf16x3", {}), ("tf32", {}), ("bf16x3+refine2", {"refine_eigen": 2}),
+         ("bf16x3+share", {"share_frames": 1}), ("bf16x3+vectors", {"propagate_vectors": 1})]
 
 
 @pytest.mark.parametrize("nmol", [512, 1024])
