@@ -153,7 +153,8 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
 // reflectors (in a.A) to Q; Q is overwritten, P and U are scratch (a.mstride floats per
 // matrix), a.Z holds the blocks' T^T V^T.
 cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, float *U, int nmat, cudaStream_t s,
-                                     int *launches);
+                                     int *launches,
+                                     bool q_split = false);
 // FP64 refinement of eigenpairs (k_refine.cu): iters steps on the eigenvectors Z (row j =
 // eigenvector j, mstride / ld as A) of the matrices H (same strides) with eigenvalues w
 // (stride wstride), chunk matrices at a time in ws (cir_refine_bytes(n, ld) per matrix).
@@ -180,6 +181,9 @@ struct GemmArgs {
     int wstride;
     float dt_over_hbar;
     int *err;              // tensor-core kernels: set to 1 when a bounded wait gives up
+    // k_tc_gemm only, epilogue 0: when set, C is written as a BF16 hi/lo pair at the same
+    // element offsets instead (batch stride 2 sC elements)
+    __nv_bfloat16 *Chi, *Clo;
 };
 // SIMT tile shapes: 128 x 128 x 8, or 64 x 64 x 16 (more blocks for small products)
 constexpr int CIR_GEMM_TILE_128 = 0, CIR_GEMM_TILE_64 = 1;

@@ -628,20 +628,23 @@ static cudaError_t backtransform_paired(const EighArgs &a, const SplitMat &Qs, c
 // (in P's buffer); the prep writes V_b (into Q's buffer) and Y_b^T (into a.Z) as pairs; P_b
 // goes to U; the updates of Qs stay split and the last one writes V in FP32 into a.A.
 static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, float *U, int nmat, int nblk,
-                                       cudaStream_t s, int &nl) {
+                                       cudaStream_t s, int &nl, bool q_split) {
     const int n = a.n, ld = a.ld, nrefl = n - 2;
     const long long ms = a.mstride, ss = 2 * a.mstride;   // per-matrix stride of a pair (BF16 elements)
     auto pair = [&](float *buf) {
         __nv_bfloat16 *b = reinterpret_cast<__nv_bfloat16 *>(buf);
         return SplitMat{b, b + ms};
     };
-    const SplitMat Qs = pair(P), Vs = pair(Q), Ys = pair(a.Z), Ps = pair(U);
-    k_bt_split_q<<<dim3((n + BT_SQ_ROWS - 1) / BT_SQ_ROWS, nmat), 256, 0, s>>>(Q, ms, n, ld, Qs, ss);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    // q_split: Q arrives as a pair already (the top merge's product wrote it so) and P is free
+    const SplitMat Qs = q_split ? pair(Q) : pair(P), Vs = q_split ? pair(P) : pair(Q), Ys = pair(a.Z), Ps = pair(U);
+    cudaError_t e = cudaSuccess;
+    if (!q_split) {
+        k_bt_split_q<<<dim3((n + BT_SQ_ROWS - 1) / BT_SQ_ROWS, nmat), 256, 0, s>>>(Q, ms, n, ld, Qs, ss);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     const int bw = min(BT_NB, (nrefl + 7) & ~7);   // width of P and of the Y_b^T blocks (<= ld)
     BtSplit sp{Vs, Ys, ld, bw, ss, ss};
-    nl += 1;
+    if (!q_split) nl += 1;
     if (bt_tc_enabled() && bt_pair_enabled() && bw == BT_NB) {
         e = backtransform_paired(a, Qs, Vs, Ys, U, nmat, nblk, s, nl);
         if (e != cudaErrorNotSupported) return e;
@@ -733,16 +736,17 @@ static cudaError_t backtransform_split(const EighArgs &a, float *Q, float *P, fl
 // matrix) is overwritten; P and U are scratch of a.mstride floats per matrix; a.Z receives Y.
 // a.A must hold the reflectors of the tridiagonalisation.
 cudaError_t cir_launch_backtransform(const EighArgs &a, float *Q, float *P, float *U, int nmat, cudaStream_t s,
-                                     int *launches) {
+                                     int *launches, bool q_split) {
     const int n = a.n, ld = a.ld, nrefl = n - 2;
     if ((ld & 3) || (reinterpret_cast<uintptr_t>(a.A) & 15) || (reinterpret_cast<uintptr_t>(a.Z) & 15))
         return cudaErrorInvalidValue;
     if (nrefl <= 0)
         return cudaMemcpyAsync(a.A, Q, sizeof(float) * (size_t)nmat * a.mstride, cudaMemcpyDeviceToDevice, s);
     const int nblk = (nrefl + BT_NB - 1) / BT_NB;
+    if (q_split && !(a.precision == CIR_PREC_BF16X3 && (ld & 7) == 0)) return cudaErrorInvalidValue;
     if (a.precision == CIR_PREC_BF16X3 && (ld & 7) == 0) {
         int nl = 0;
-        const cudaError_t e = backtransform_split(a, Q, P, U, nmat, nblk, s, nl);
+        const cudaError_t e = backtransform_split(a, Q, P, U, nmat, nblk, s, nl, q_split);
         if (launches) *launches += nl;
         return e;
     }

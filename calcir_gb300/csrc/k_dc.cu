@@ -26,6 +26,8 @@
 // applied to Q_T in compact WY blocks (k_backtransform.cu): FP32 GEMMs in the plain form,
 // the tensor-core GEMM (a.precision) in the mixed forms.
 #include "cir_device.cuh"
+
+#include <cstdlib>
 #include <float.h>
 
 namespace {
@@ -551,6 +553,15 @@ __global__ void __launch_bounds__(256) k_dc_finish(EighArgs a) {
     }
 }
 
+// CIR_Q_PAIR=0: the top merge writes Q_T in FP32 and the back-transform splits it (for comparison)
+bool pair_q_enabled() {
+    static const bool on = [] {
+        const char *v = getenv("CIR_Q_PAIR");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 int dc_depth(int n) {
     int D = 0;
     while (((n + (1 << D) - 1) >> D) > DC_LEAF) D++;
@@ -574,6 +585,10 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
     if (e != cudaSuccess) return e;
     int nl = 1;
     int cur = 0;
+    // the split-BF16 back-transform takes Q_T as a BF16 pair: the top merge's tensor-core
+    // product writes it so directly, and the back-transform skips its own split of Q_T
+    const bool q_pair = a.precision == CIR_PREC_BF16X3 && (ld & 7) == 0 && n > 2 && pair_q_enabled();
+    bool q_split = false;
     for (int level = D - 1; level >= 0; level--) {
         const int KM = ((n + (1 << level) - 1) >> level);
         const DcSmem L(KM);
@@ -613,12 +628,18 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
                     g.a_colmajor = true;
                     g.epilogue = 0;
                     g.err = a.err;
+                    if (level == 0 && q_pair) {
+                        __nv_bfloat16 *pb = reinterpret_cast<__nv_bfloat16 *>(buf[other]) + (size_t)a0 * ld + h0;
+                        g.Chi = pb;
+                        g.Clo = pb + a.mstride;
+                    }
                     e = cir_launch_tc_gemm(g, nmat, a.precision, s, nullptr);
                     if (e != cudaSuccess) return e;
                     nl++;
                 }
             }
             nl++;
+            if (level == 0 && q_pair) q_split = true;
         } else {
             const int tiles = ((KM / 2 + 1 + 63) / 64) * ((KM + 63) / 64);
             k_dc_gemm<<<dim3(tiles * (1 << level) * 2, nmat), 256, 0, s>>>(a, level, tiles, buf[cur], buf[2], buf[other]);
@@ -630,7 +651,7 @@ cudaError_t cir_launch_dc(const EighArgs &a, int nmat, cudaStream_t s, int *laun
     }
     // V = Q_H Q_T into a.A: the reflectors applied to Q_T (buf[cur]) in compact WY blocks,
     // with the free ping-pong buffer as scratch
-    e = cir_launch_backtransform(a, buf[cur], buf[cur ^ 1], buf[2], nmat, s, &nl);
+    e = cir_launch_backtransform(a, buf[cur], buf[cur ^ 1], buf[2], nmat, s, &nl, q_split);
     if (e != cudaSuccess) return e;
     // optional FP64 refinement of the eigenpairs (eigenvalues in DE row 0) before W and the
     // distributions are written

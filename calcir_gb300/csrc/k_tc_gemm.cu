@@ -267,6 +267,33 @@ __global__ void __launch_bounds__(NTHREADS) k_tc_gemm(GemmArgs g) {
                 #pragma unroll
                 for (int q = 0; q < 16; q++) v[q] = (c + q < g.N ? d[q] : 0.f) - v[q];
             }
+            if (g.Chi) {   // as a BF16 hi/lo pair
+                const size_t o = (size_t)bz * 2 * g.sC + (size_t)r * g.ldc + c;
+                __nv_bfloat16 *ph = g.Chi + o, *pl = g.Clo + o;
+                if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(ph) | reinterpret_cast<uintptr_t>(pl)) & 15) == 0) {
+                    uint32_t wh[8], wl[8];
+                    #pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(v[q], v[q + 1]);
+                        const __nv_bfloat162 l = __floats2bfloat162_rn(v[q] - __bfloat162float(h.x), v[q + 1] - __bfloat162float(h.y));
+                        wh[q / 2] = *reinterpret_cast<const uint32_t *>(&h);
+                        wl[q / 2] = *reinterpret_cast<const uint32_t *>(&l);
+                    }
+                    *reinterpret_cast<uint4 *>(ph) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+                    *reinterpret_cast<uint4 *>(ph + 8) = make_uint4(wh[4], wh[5], wh[6], wh[7]);
+                    *reinterpret_cast<uint4 *>(pl) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+                    *reinterpret_cast<uint4 *>(pl + 8) = make_uint4(wl[4], wl[5], wl[6], wl[7]);
+                } else {
+                    #pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        if (c + q < g.N) {
+                            const __nv_bfloat16 h = __float2bfloat16_rn(v[q]);
+                            ph[q] = h;
+                            pl[q] = __float2bfloat16_rn(v[q] - __bfloat162float(h));
+                        }
+                }
+                continue;
+            }
             float *p = C + (size_t)r * g.ldc + c;
             if (c + 15 < g.N && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
                 #pragma unroll
