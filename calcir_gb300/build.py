@@ -23,7 +23,7 @@ EXE = os.path.join(HERE, "calcir")
 CU = ["k_hamiltonian.cu", "k_eigh.cu", "k_dc.cu", "k_backtransform.cu", "k_adjoint.cu", "k_gemm.cu", "k_tc_gemm.cu", "k_tc_split.cu", "k_refine.cu", "k_tcf.cu", "k_fft.cu", "k_sbr.cu", "cir_api.cu"]
 CPP = ["host_params.cpp", "host_synth.cpp", "host_traj.cpp", "host_xtc.cpp"]
 MAIN = "calcir_main.cpp"
-HEADERS = ["cir_device.cuh", "cir_internal.h"]
+HEADERS = ["cir_device.cuh", "cir_internal.h", "cir_plan.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -14,6 +14,7 @@
 // every one of the 15 correlation dot products returns a scalar to the host.  Here
 // nothing leaves the device until the job ends.
 #include "cir_device.cuh"
+#include "cir_plan.h"
 
 #include <cmath>
 #include <cstdio>
@@ -854,31 +855,7 @@ static int tridiag_wave(cir_ctx *c, int n) {
     return std::max(1, sms * blocks);
 }
 
-// Chunk length for K steps of St origins, at most kn_max steps a chunk.  The
-// tridiagonalisation runs `wave` matrices at a time, and a chunk whose last wave is nearly
-// empty pays for about a third of a wave while its few blocks run alone (order 1024 at 456
-// resident blocks: 3232 matrices, 7.09 waves, 525 ms; 3168 matrices, 6.95 waves, 501 ms).
-// Of the chunkings into as few chunks as kn_max allows, equal in length but the last, the
-// one with the least estimated time is taken: whole waves, a part-filled last wave counted
-// as at least 0.3 of one; ties go to the longer chunks.
-static int plan_chunk(int K, int St, int kn_max, int wave) {
-    kn_max = std::max(1, std::min(kn_max, K));
-    const int nc = (K + kn_max - 1) / kn_max, kn_min = (K + nc - 1) / nc;
-    double best = 1e300;
-    int pick = kn_max;
-    for (int kn = kn_max; kn >= kn_min; kn--) {
-        double cost = 0.0;
-        for (int k0 = 0; k0 < K && cost < best; k0 += kn) {
-            const double w = (double)St * std::min(kn, K - k0) / wave, f = w - std::floor(w);
-            cost += std::floor(w) + (f > 0.0 ? std::max(f, 0.3) : 0.0);
-        }
-        if (cost < best - 1e-9) {
-            best = cost;
-            pick = kn;
-        }
-    }
-    return pick;
-}
+static int plan_chunk(int K, int St, int kn_max, int wave) { return cir_plan_chunk(K, St, kn_max, wave); }
 
 // One group's job: ntraj trajectories of one size, nsamples origins each, batched through
 // every launch.  dxyz / dbox hold all the group's frames on the device; fidx[(t*S + s)*K + k]
@@ -1236,8 +1213,7 @@ struct GroupJob {
         int hA = 0;   // the first part: whole waves of the tridiagonalisation, all but the last one
         if (may_split && !skip_tq && eig_split_enabled() && !e.Href && !e.phase_ns &&
             (e.hist_group == 0 || e.hist_group >= nmat)) {
-            const int wave = tridiag_wave(c, n);
-            if (nmat >= 2 * wave) hA = (nmat / wave - 1) * wave;
+            hA = cir_split_first_part(nmat, tridiag_wave(c, n));
         }
         if (hA > 0 && hA < nmat) {
             // the batch in two parts on two streams: the first (whole waves) on the library
